@@ -1,0 +1,31 @@
+"""GPU engine for dust2's data-parallel hot path, with a Python mirror of
+dust2's R verbs.  The engine itself is the CUDA library built from
+csrc/ (C ABI: include/dust2_gb300.h)."""
+
+from ._lib import DustError, device_count
+from .interface import (
+    DustLikelihood, DustSystem, Generator, dust_filter_create,
+    dust_filter_data, dust_likelihood_last_state, dust_likelihood_rng_state,
+    dust_likelihood_run, dust_likelihood_serial_fallbacks,
+    dust_likelihood_set_rng_state, dust_ode_control,
+    dust_system_compare_data, dust_system_create, dust_system_internals,
+    dust_system_reorder, dust_system_rng_state, dust_system_run_to_time,
+    dust_system_set_rng_state, dust_system_set_state,
+    dust_system_set_state_initial, dust_system_set_time,
+    dust_system_simulate, dust_system_state, dust_system_time,
+    dust_system_update_pars, logistic, rng_streams, seir_age, sir, sir_cases,
+    sirode, walk)
+
+__all__ = [
+    "DustError", "DustLikelihood", "DustSystem", "Generator",
+    "device_count", "dust_filter_create", "dust_filter_data",
+    "dust_likelihood_last_state", "dust_likelihood_rng_state",
+    "dust_likelihood_run", "dust_likelihood_serial_fallbacks",
+    "dust_likelihood_set_rng_state", "dust_ode_control",
+    "dust_system_compare_data", "dust_system_create",
+    "dust_system_internals", "dust_system_reorder", "dust_system_rng_state",
+    "dust_system_run_to_time", "dust_system_set_rng_state",
+    "dust_system_set_state", "dust_system_set_state_initial",
+    "dust_system_set_time", "dust_system_simulate", "dust_system_state",
+    "dust_system_time", "dust_system_update_pars", "logistic", "rng_streams",
+    "seir_age", "sir", "sir_cases", "sirode", "walk"]

@@ -1,0 +1,699 @@
+// The extern "C" entry points declared in include/dust2_gb300.h.  Each
+// one validates its arguments the way dust2's R adaptors do
+// (inst/include/dust2/r/*.hpp), forwards to the type-erased engine, and
+// turns exceptions into a status code plus a thread-local message.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/dust2_gb300.h"
+#include "dust2gpu/random.hpp"
+#include "engine/api.hpp"
+#include "engine/registry.hpp"
+#include "engine/seeding.hpp"
+
+struct dust2_gb300_system {
+  std::unique_ptr<dust2gpu::engine::system_api> impl;
+};
+
+struct dust2_gb300_filter {
+  std::unique_ptr<dust2gpu::engine::filter_api> impl;
+  std::vector<int> last_index_group;
+};
+
+namespace dust2gpu {
+namespace engine {
+
+namespace {
+
+std::map<std::string, const system_factory*>& registry() {
+  static std::map<std::string, const system_factory*> r;
+  return r;
+}
+
+std::mutex& registry_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+}  // namespace
+
+void register_system(const system_factory* f) {
+  std::lock_guard<std::mutex> lock(registry_mutex());
+  registry()[f->name] = f;
+}
+
+const system_factory* find_system(const char* name) {
+  std::lock_guard<std::mutex> lock(registry_mutex());
+  auto it = registry().find(name == nullptr ? "" : name);
+  if (it == registry().end()) {
+    throw std::runtime_error(std::string("Unknown system '") +
+                             (name == nullptr ? "" : name) + "'");
+  }
+  return it->second;
+}
+
+std::vector<const system_factory*> all_systems() {
+  std::lock_guard<std::mutex> lock(registry_mutex());
+  std::vector<const system_factory*> ret;
+  for (auto& el : registry()) {
+    ret.push_back(el.second);
+  }
+  return ret;
+}
+
+}  // namespace engine
+}  // namespace dust2gpu
+
+namespace {
+
+using dust2gpu::engine::filter_api;
+using dust2gpu::engine::system_api;
+
+thread_local std::string last_error;
+
+template <typename F>
+int guard(F f) {
+  try {
+    f();
+    return DUST2_GB300_OK;
+  } catch (const std::exception& e) {
+    last_error = e.what();
+  } catch (...) {
+    last_error = "unknown error";
+  }
+  return DUST2_GB300_ERROR;
+}
+
+void need(bool ok, const char* msg) {
+  if (!ok) {
+    throw std::runtime_error(msg);
+  }
+}
+
+// r/system.hpp:66-73
+void check_errors(system_api& sys, const char* action) {
+  if (sys.errors_pending()) {
+    throw std::runtime_error(std::string("Can't currently ") + action +
+                             " this system: errors are pending");
+  }
+}
+
+// Stream block from a seed (see the header for the accepted forms).
+std::vector<std::uint64_t> seed_streams(const std::uint64_t* seed,
+                                        std::size_t seed_len,
+                                        std::size_t n_streams) {
+  need(seed != nullptr && seed_len > 0, "A seed is required");
+  if (seed_len == 1) {
+    return dust2gpu::engine::make_streams_from_seed(seed[0], n_streams);
+  }
+  if (seed_len % 4 != 0) {
+    throw std::runtime_error(
+      "Expected a seed of 1 word or a multiple of 4 words (32 bytes per "
+      "stream)");
+  }
+  const std::size_t given = seed_len / 4;
+  if (given >= n_streams) {
+    return std::vector<std::uint64_t>(seed, seed + 4 * n_streams);
+  }
+  auto tail = dust2gpu::engine::make_streams(seed + 4 * (given - 1),
+                                             n_streams - given + 1);
+  std::vector<std::uint64_t> ret(seed, seed + 4 * given);
+  ret.insert(ret.end(), tail.begin() + 4, tail.end());
+  return ret;
+}
+
+dust2gpu::engine::ode_control to_control(const dust2_gb300_ode_control* c) {
+  dust2gpu::engine::ode_control ctl;
+  if (c != nullptr) {
+    ctl.max_steps = c->max_steps;
+    ctl.atol = c->atol;
+    ctl.rtol = c->rtol;
+    ctl.step_size_min = c->step_size_min;
+    ctl.step_size_max = c->step_size_max;
+    if (c->critical_times != nullptr) {
+      ctl.critical_times.assign(c->critical_times,
+                                c->critical_times + c->n_critical_times);
+    }
+    ctl.debug_record_step_times = c->debug_record_step_times != 0;
+  }
+  // r/continuous/control.hpp:15-17
+  ctl.step_size_min = std::max(ctl.step_size_min,
+                               std::numeric_limits<double>::epsilon());
+  return ctl;
+}
+
+std::vector<int> to_int_index(const std::size_t* index, std::size_t n,
+                              std::size_t max, const char* name) {
+  std::vector<int> ret;
+  if (index == nullptr) {
+    return ret;
+  }
+  for (std::size_t i = 0; i < n; ++i) {
+    if (index[i] >= max) {
+      char buf[256];
+      std::snprintf(buf, sizeof(buf),
+                    "All values of '%s' must be in [1, %zu], but '%s[%zu]' "
+                    "was %zu", name, max, name, i + 1, index[i] + 1);
+      throw std::runtime_error(buf);
+    }
+    ret.push_back(static_cast<int>(index[i]));
+  }
+  return ret;
+}
+
+system_api& sysref(dust2_gb300_system* sys) {
+  need(sys != nullptr && sys->impl != nullptr, "Invalid system handle");
+  return *sys->impl;
+}
+
+filter_api& filref(dust2_gb300_filter* f) {
+  need(f != nullptr && f->impl != nullptr, "Invalid filter handle");
+  return *f->impl;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dust2_gb300_abi_version(void) {
+  return 1;
+}
+
+size_t dust2_gb300_last_error(char* buf, size_t len) {
+  if (buf != nullptr && len > 0) {
+    const std::size_t n = std::min(len - 1, last_error.size());
+    std::memcpy(buf, last_error.data(), n);
+    buf[n] = '\0';
+  }
+  return last_error.size();
+}
+
+int dust2_gb300_device_count(int32_t* n) {
+  return guard([&] {
+    int c = 0;
+    const cudaError_t err = cudaGetDeviceCount(&c);
+    if (err != cudaSuccess) {
+      cudaGetLastError();
+      c = 0;
+    }
+    *n = c;
+  });
+}
+
+int dust2_gb300_systems(char* buf, size_t len) {
+  return guard([&] {
+    std::string s;
+    for (auto* f : dust2gpu::engine::all_systems()) {
+      s += (s.empty() ? "" : ",") + std::string(f->name);
+    }
+    need(buf != nullptr && len > s.size(), "buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+  });
+}
+
+int dust2_gb300_system_info(const char* name, char* json, size_t len) {
+  return guard([&] {
+    const auto* f = dust2gpu::engine::find_system(name);
+    const std::string s = f->info_json();
+    need(json != nullptr && len > s.size(), "buffer too small");
+    std::memcpy(json, s.c_str(), s.size() + 1);
+  });
+}
+
+int dust2_gb300_rng_streams(const uint64_t* seed, size_t seed_len,
+                            size_t n_streams, uint64_t* out) {
+  return guard([&] {
+    const auto words = seed_streams(seed, seed_len, n_streams);
+    std::copy(words.begin(), words.end(), out);
+  });
+}
+
+int dust2_gb300_system_alloc(const char* name, const double* pars,
+                             size_t n_groups, size_t n_particles,
+                             double time, double dt,
+                             const dust2_gb300_ode_control* control,
+                             const uint64_t* seed, size_t seed_len,
+                             int32_t deterministic,
+                             dust2_gb300_system** out) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    need(n_particles >= 1, "'n_particles' must be at least 1");
+    need(n_groups >= 1, "'n_groups' must be at least 1");
+    const auto* f = dust2gpu::engine::find_system(name);
+    if (!f->continuous) {
+      need(dt > 0, "Expected 'dt' to be greater than 0");
+    }
+    const std::size_t n_total = n_particles * n_groups;
+    auto words = seed_streams(seed, seed_len, n_total);
+    std::vector<int> np(n_groups, static_cast<int>(n_particles));
+    auto ctl = to_control(control);
+    auto* impl = f->create_system(pars, static_cast<int>(n_groups), np, time,
+                                  dt, ctl, words, deterministic != 0, 0);
+    *out = new dust2_gb300_system{std::unique_ptr<system_api>(impl)};
+  });
+}
+
+int dust2_gb300_system_free(dust2_gb300_system* sys) {
+  return guard([&] { delete sys; });
+}
+
+int dust2_gb300_system_dim(const dust2_gb300_system* sys, size_t* n_state,
+                           size_t* n_particles, size_t* n_groups) {
+  return guard([&] {
+    need(sys != nullptr && sys->impl != nullptr, "Invalid system handle");
+    *n_state = sys->impl->n_state();
+    *n_particles = sys->impl->n_particles()[0];
+    *n_groups = sys->impl->n_groups();
+  });
+}
+
+int dust2_gb300_system_state(dust2_gb300_system* sys, double* out) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "get state from");
+    s.get_state(out);
+  });
+}
+
+int dust2_gb300_system_set_state(dust2_gb300_system* sys, const double* value,
+                                 const size_t* index_state, size_t n_index_state,
+                                 const size_t* index_particle,
+                                 size_t n_index_particle,
+                                 const size_t* index_group, size_t n_index_group,
+                                 int32_t recycle_particle,
+                                 int32_t recycle_group) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    const std::size_t n_state = s.n_state();
+    const std::size_t n_particles = s.n_particles()[0];
+    const std::size_t n_groups = s.n_groups();
+    auto is = to_int_index(index_state, n_index_state, n_state, "index_state");
+    auto ip = to_int_index(index_particle, n_index_particle, n_particles,
+                           "index_particle");
+    auto ig = to_int_index(index_group, n_index_group, n_groups,
+                           "index_group");
+    std::vector<double> state(n_state * n_particles * n_groups);
+    const bool simple = is.empty() && ip.empty() && ig.empty() &&
+      !recycle_particle && !recycle_group;
+    if (simple) {
+      std::copy_n(value, state.size(), state.begin());
+    } else {
+      // internals.hpp:110-163
+      s.get_state(state.data());
+      const std::size_t n_state_in = is.empty() ? n_state : is.size();
+      const std::size_t n_particles_in = ip.empty() ? n_particles : ip.size();
+      const std::size_t n_groups_in = ig.empty() ? n_groups : ig.size();
+      const std::size_t off_particle = recycle_particle ? 0 : n_state_in;
+      const std::size_t off_group = recycle_group ? 0 :
+        (n_state_in * (recycle_particle ? 1 : n_particles_in));
+      for (std::size_t i = 0; i < n_groups_in; ++i) {
+        for (std::size_t j = 0; j < n_particles_in; ++j) {
+          const std::size_t src = i * off_group + j * off_particle;
+          const std::size_t gi = ig.empty() ? i : ig[i];
+          const std::size_t pj = ip.empty() ? j : ip[j];
+          const std::size_t dst = (n_particles * gi + pj) * n_state;
+          if (!is.empty()) {
+            for (std::size_t k = 0; k < n_state_in; ++k) {
+              state[dst + is[k]] = value[src + k];
+            }
+          } else {
+            std::copy_n(value + src, n_state, state.begin() + dst);
+          }
+        }
+      }
+    }
+    s.put_state(state.data());
+  });
+}
+
+int dust2_gb300_system_set_state_initial(dust2_gb300_system* sys) {
+  return guard([&] { sysref(sys).set_state_initial(); });
+}
+
+int dust2_gb300_system_time(dust2_gb300_system* sys, double* time) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "get time from");
+    *time = s.time();
+  });
+}
+
+int dust2_gb300_system_set_time(dust2_gb300_system* sys, double time) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "set time for");
+    s.set_time(time);
+  });
+}
+
+int dust2_gb300_system_rng_state(dust2_gb300_system* sys, uint64_t* out) {
+  return guard([&] { sysref(sys).get_rng_state(out); });
+}
+
+int dust2_gb300_system_set_rng_state(dust2_gb300_system* sys,
+                                     const uint64_t* state, size_t len) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    const std::size_t expected = 4 * static_cast<std::size_t>(
+      s.n_particles_total());
+    if (len != expected) {
+      char buf[200];
+      std::snprintf(buf, sizeof(buf),
+                    "Incorrect length for 'rng_state'; expected %zu but "
+                    "given %zu", expected * 8, len * 8);
+      throw std::runtime_error(buf);
+    }
+    s.put_rng_state(state);
+  });
+}
+
+int dust2_gb300_system_update_pars(dust2_gb300_system* sys,
+                                   const double* pars,
+                                   const size_t* index_group,
+                                   size_t n_index_group) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    auto ig = to_int_index(index_group, n_index_group, s.n_groups(),
+                           "index_group");
+    if (ig.empty()) {
+      s.update_pars(pars, nullptr, 0);
+    } else {
+      s.update_pars(pars, ig.data(), static_cast<int>(ig.size()));
+    }
+  });
+}
+
+int dust2_gb300_system_run_to_time(dust2_gb300_system* sys, double time) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "run");
+    const double curr = s.time();
+    if (time < curr) {
+      char buf[200];
+      std::snprintf(buf, sizeof(buf),
+                    "Can't run to time %f, system already at time %f", time,
+                    curr);
+      throw std::runtime_error(buf);
+    }
+    s.run_to_time(time);
+  });
+}
+
+int dust2_gb300_system_simulate(dust2_gb300_system* sys, const double* times,
+                                size_t n_times, const size_t* index_state,
+                                size_t n_index_state, double* out) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "simulate");
+    need(n_times >= 1, "Expected at least one value in 'times'");
+    if (times[0] < s.time()) {
+      char buf[200];
+      std::snprintf(buf, sizeof(buf),
+                    "Expected 'time[1]' (%d) to be larger than the previous "
+                    "value (%d)", static_cast<int>(times[0]),
+                    static_cast<int>(s.time()));
+      throw std::runtime_error(buf);
+    }
+    for (std::size_t i = 1; i < n_times; ++i) {
+      need(times[i] > times[i - 1], "Values in 'times' must be increasing");
+    }
+    auto is = to_int_index(index_state, n_index_state, s.n_state(),
+                           "index_state");
+    s.simulate(times, static_cast<int>(n_times), is.empty() ? nullptr : is.data(),
+               static_cast<int>(is.size()), out);
+  });
+}
+
+int dust2_gb300_system_reorder(dust2_gb300_system* sys, const size_t* index,
+                               size_t len) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "reorder");
+    const std::size_t n_particles = s.n_particles()[0];
+    const std::size_t n_total = s.n_particles_total();
+    if (len != n_total) {
+      throw std::runtime_error("Expected an index of length " +
+                               std::to_string(n_total));
+    }
+    std::vector<int> idx(len);
+    for (std::size_t i = 0; i < len; ++i) {
+      if (index[i] >= n_particles) {
+        throw std::runtime_error("Expected 'index' values to lie in [1, " +
+                                 std::to_string(n_particles) + "]");
+      }
+      idx[i] = static_cast<int>(index[i]);
+    }
+    s.reorder(idx.data());
+  });
+}
+
+int dust2_gb300_system_compare_data(dust2_gb300_system* sys,
+                                    const double* data, size_t n_groups_data,
+                                    double* out) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_errors(s, "compare data for");
+    if (!s.has_compare()) {
+      throw std::runtime_error(
+        std::string("Can't compare against data; the '") + s.name() +
+        "' system does not have 'compare_data'");
+    }
+    if (n_groups_data != 1 &&
+        n_groups_data != static_cast<std::size_t>(s.n_groups())) {
+      throw std::runtime_error(
+        "Expected 'data' to have length " + std::to_string(s.n_groups()) +
+        ", but it had length " + std::to_string(n_groups_data));
+    }
+    s.compare_data(data, static_cast<int>(n_groups_data), out);
+  });
+}
+
+int dust2_gb300_system_internals(dust2_gb300_system* sys, double* step_size,
+                                 double* error, int64_t* n_steps,
+                                 int64_t* n_steps_accepted,
+                                 int64_t* n_steps_rejected) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    need(s.is_continuous(), "discrete-time systems have no internals");
+    const auto rows = s.ode_internals();
+    for (std::size_t k = 0; k < rows.size(); ++k) {
+      step_size[k] = rows[k].step_size;
+      error[k] = rows[k].error;
+      n_steps[k] = rows[k].n_steps;
+      n_steps_accepted[k] = rows[k].n_steps_accepted;
+      n_steps_rejected[k] = rows[k].n_steps_rejected;
+    }
+  });
+}
+
+int dust2_gb300_system_step_times(dust2_gb300_system* sys, size_t particle,
+                                  double* out, size_t cap, size_t* n) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    need(s.is_continuous(), "discrete-time systems have no step times");
+    const auto times = s.ode_step_times();
+    need(particle < times.size(), "particle out of range");
+    const auto& t = times[particle];
+    *n = t.size();
+    for (std::size_t i = 0; i < std::min(cap, t.size()); ++i) {
+      out[i] = t[i];
+    }
+  });
+}
+
+static int filter_alloc_impl(const char* name, const double* pars,
+                             size_t n_groups, const std::vector<int>& np,
+                             double time_start, const double* time,
+                             size_t n_time, const double* data,
+                             size_t n_groups_data, double dt,
+                             const uint64_t* seed, size_t seed_len,
+                             dust2_gb300_filter** out) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    need(n_groups >= 1, "'n_groups' must be at least 1");
+    need(n_time >= 1, "Expected 'data' to have at least one row");
+    need(dt > 0, "Expected 'dt' to be greater than 0");
+    need(n_groups_data == 1 || n_groups_data == n_groups,
+         "Expected 'data' to have 1 or n_groups groups");
+    // r/helpers.hpp check_time_sequence(require_later = true)
+    if (time[0] <= time_start) {
+      char buf[200];
+      std::snprintf(buf, sizeof(buf),
+                    "'time_start' (%g) is later than the first time in "
+                    "'data' (%g)", time_start, time[0]);
+      if (time[0] < time_start) {
+        throw std::runtime_error(buf);
+      }
+    }
+    for (std::size_t i = 1; i < n_time; ++i) {
+      need(time[i] > time[i - 1], "Values in 'time' must be increasing");
+    }
+    const auto* f = dust2gpu::engine::find_system(name);
+    std::size_t n_streams = 0;
+    for (auto n : np) {
+      need(n >= 1, "'n_particles' must be at least 1");
+      n_streams += static_cast<std::size_t>(n) + 2;
+    }
+    auto words = seed_streams(seed, seed_len, n_streams);
+    auto* impl = f->create_filter(pars, static_cast<int>(n_groups), np,
+                                  time_start, time, static_cast<int>(n_time),
+                                  data, static_cast<int>(n_groups_data), dt,
+                                  words, 0);
+    *out = new dust2_gb300_filter{std::unique_ptr<filter_api>(impl), {}};
+  });
+}
+
+int dust2_gb300_filter_alloc(const char* name, const double* pars,
+                             size_t n_groups, size_t n_particles,
+                             double time_start, const double* time,
+                             size_t n_time, const double* data,
+                             size_t n_groups_data, double dt,
+                             const uint64_t* seed, size_t seed_len,
+                             dust2_gb300_filter** out) {
+  std::vector<int> np(n_groups, static_cast<int>(n_particles));
+  return filter_alloc_impl(name, pars, n_groups, np, time_start, time, n_time,
+                           data, n_groups_data, dt, seed, seed_len, out);
+}
+
+int dust2_gb300_filter_alloc_uneven(const char* name, const double* pars,
+                                    size_t n_groups,
+                                    const size_t* n_particles,
+                                    double time_start, const double* time,
+                                    size_t n_time, const double* data,
+                                    size_t n_groups_data, double dt,
+                                    const uint64_t* seed, size_t seed_len,
+                                    dust2_gb300_filter** out) {
+  std::vector<int> np;
+  for (std::size_t g = 0; g < n_groups; ++g) {
+    np.push_back(static_cast<int>(n_particles[g]));
+  }
+  return filter_alloc_impl(name, pars, n_groups, np, time_start, time, n_time,
+                           data, n_groups_data, dt, seed, seed_len, out);
+}
+
+int dust2_gb300_filter_free(dust2_gb300_filter* filter) {
+  return guard([&] { delete filter; });
+}
+
+int dust2_gb300_filter_dim(const dust2_gb300_filter* filter, size_t* n_state,
+                           size_t* n_particles_total, size_t* n_groups,
+                           size_t* n_time) {
+  return guard([&] {
+    need(filter != nullptr && filter->impl != nullptr,
+         "Invalid filter handle");
+    auto& s = filter->impl->sys();
+    *n_state = s.n_state();
+    *n_particles_total = s.n_particles_total();
+    *n_groups = s.n_groups();
+    *n_time = filter->impl->n_times();
+  });
+}
+
+int dust2_gb300_filter_run(dust2_gb300_filter* filter, const double* initial,
+                           const size_t* index_group, size_t n_index_group,
+                           double* ll) {
+  return guard([&] {
+    auto& f = filref(filter);
+    auto ig = to_int_index(index_group, n_index_group, f.sys().n_groups(),
+                           "index_group");
+    f.run(initial, ig.empty() ? nullptr : ig.data(),
+          static_cast<int>(ig.size()), ll);
+    filter->last_index_group = ig;
+  });
+}
+
+int dust2_gb300_filter_update_pars(dust2_gb300_filter* filter,
+                                   const double* pars,
+                                   const size_t* index_group,
+                                   size_t n_index_group) {
+  return guard([&] {
+    auto& f = filref(filter);
+    auto ig = to_int_index(index_group, n_index_group, f.sys().n_groups(),
+                           "index_group");
+    f.update_pars(pars, ig.empty() ? nullptr : ig.data(),
+                  static_cast<int>(ig.size()));
+  });
+}
+
+int dust2_gb300_filter_rng_state(dust2_gb300_filter* filter, uint64_t* out,
+                                 size_t len) {
+  return guard([&] {
+    auto& f = filref(filter);
+    need(len == 4 * f.n_rng_streams(), "rng buffer has the wrong length");
+    f.get_rng_state(out);
+  });
+}
+
+int dust2_gb300_filter_set_rng_state(dust2_gb300_filter* filter,
+                                     const uint64_t* state, size_t len) {
+  return guard([&] {
+    auto& f = filref(filter);
+    const std::size_t expected = 4 * f.n_rng_streams();
+    if (len != expected) {
+      char buf[200];
+      std::snprintf(buf, sizeof(buf),
+                    "Incorrect length for 'rng_state'; expected %zu but "
+                    "given %zu", expected * 8, len * 8);
+      throw std::runtime_error(buf);
+    }
+    f.put_rng_state(state);
+  });
+}
+
+int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
+                                  int32_t select_random_particle,
+                                  double* out) {
+  return guard([&] {
+    auto& f = filref(filter);
+    need(f.has_run(), "State is not current");
+    auto& s = f.sys();
+    const std::size_t n_state = s.n_state();
+    std::vector<double> state(n_state * s.n_particles_total());
+    s.get_state(state.data());
+    std::vector<int> groups = filter->last_index_group;
+    if (groups.empty()) {
+      for (int g = 0; g < s.n_groups(); ++g) {
+        groups.push_back(g);
+      }
+    }
+    std::vector<int> offset(s.n_groups(), 0);
+    for (int g = 1; g < s.n_groups(); ++g) {
+      offset[g] = offset[g - 1] + s.n_particles()[g - 1];
+    }
+    if (select_random_particle) {
+      const auto pick = f.select_random_particle();
+      std::size_t pos = 0;
+      for (int g : groups) {
+        const std::size_t from = (offset[g] + pick[g]) * n_state;
+        std::copy_n(state.begin() + from, n_state, out + pos);
+        pos += n_state;
+      }
+    } else {
+      std::size_t pos = 0;
+      for (int g : groups) {
+        const std::size_t from = offset[g] * n_state;
+        const std::size_t n = n_state * s.n_particles()[g];
+        std::copy_n(state.begin() + from, n, out + pos);
+        pos += n;
+      }
+    }
+  });
+}
+
+int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,
+                                        int64_t* n) {
+  return guard([&] { *n = filref(filter).n_serial_fallbacks(); });
+}
+
+}  // extern "C"

@@ -1,0 +1,252 @@
+// Random variates drawn from a per-particle stream, identical on host and
+// device.
+//
+// dust2 calls these through monty (monty::random::binomial, poisson,
+// exponential_rate, normal; call sites inst/examples/sir.cpp:63-66,116,
+// walk.cpp:58,75).  monty is not available in this build, so the
+// samplers are restated here from the published algorithms monty
+// documents:
+//   binomial  inversion (Kachitvichyanukul & Schmeiser 1988, "BINV") when
+//             n * min(p, 1-p) < 10, otherwise BTRS, the transformed
+//             rejection method with squeeze of Hormann (1993), "The
+//             generation of binomial random variates", J. Stat. Comput.
+//             Simul. 46:101-110.  p > 1/2 is handled by symmetry.
+//   poisson   multiplication of uniforms (Knuth, TAOCP vol 2) when
+//             lambda < 10, otherwise PTRS, Hormann (1993), "The
+//             transformed rejection method for generating Poisson random
+//             variables", Insurance: Math. Econ. 12:39-45.
+//   exponential  inversion, -log(1 - U) / rate.
+//   normal    Box & Muller (1958), one variate per pair of uniforms.
+//
+// The constant-heavy setup of the rejection samplers (the log-factorial
+// terms of BTRS, the log terms of PTRS) only feeds the final acceptance
+// test, so it is evaluated lazily, the first time a candidate falls
+// outside the squeeze; this changes no result.
+//
+// Invalid arguments do not throw (device code cannot): the sampler
+// records the first error in the generator's error slot and returns NaN.
+// Every rejection loop is bounded so that no input can make a kernel spin.
+#pragma once
+
+#include <cmath>
+
+#include "common.hpp"
+#include "math.hpp"
+#include "random.hpp"
+
+namespace dust2gpu {
+namespace random {
+
+// Bound on candidate draws in a rejection loop; with valid arguments the
+// acceptance rate is above 0.8, so reaching this means corrupt input.
+constexpr int MAX_REJECTION_ATTEMPTS = 100000;
+// BINV restarts when the search passes this count (the published cap).
+constexpr double BINV_MAX_X = 110;
+
+DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
+  const double q = 1.0 - p;
+  const double s = p / q;
+  const double a = (n + 1.0) * s;
+  const double r0 = math::exp(n * math::log(q));  // q^n
+  for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
+    double r = r0;
+    double u = random_real(rng);
+    double x = 0;
+    while (u > r) {
+      u = u - r;
+      x = x + 1.0;
+      r = r * (a / x - s);
+      if (x > BINV_MAX_X) {
+        break;
+      }
+    }
+    if (x <= BINV_MAX_X) {
+      return x;
+    }
+  }
+  set_error(rng, ERR_BINOMIAL_INVALID, n, p);
+  return math::quiet_nan();
+}
+
+DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
+  const double q = 1.0 - p;
+  const double spq = std::sqrt(n * p * q);
+  const double b = 1.15 + 2.53 * spq;
+  const double a = -0.0873 + 0.0248 * b + 0.01 * p;
+  const double c = n * p + 0.5;
+  const double v_r = 0.92 - 4.2 / b;
+  bool have_setup = false;
+  double alpha = 0, lpq = 0, m = 0, h = 0;
+  for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
+    const double u = random_real(rng) - 0.5;
+    double v = random_real(rng);
+    const double us = 0.5 - std::fabs(u);
+    const double k = std::floor((2.0 * a / us + b) * u + c);
+    if (us >= 0.07 && v <= v_r) {
+      return k;
+    }
+    if (k < 0 || k > n) {
+      continue;
+    }
+    if (!have_setup) {
+      alpha = (2.83 + 5.1 / b) * spq;
+      lpq = math::log(p / q);
+      m = std::floor((n + 1.0) * p);
+      h = math::log_factorial(m) + math::log_factorial(n - m);
+      have_setup = true;
+    }
+    v = math::log(v * alpha / (a / (us * us) + b));
+    if (v <= h - math::log_factorial(k) - math::log_factorial(n - k) +
+        (k - m) * lpq) {
+      return k;
+    }
+  }
+  set_error(rng, ERR_BINOMIAL_INVALID, n, p);
+  return math::quiet_nan();
+}
+
+// Binomial(n, p) for integer-valued n >= 0 and p in [0, 1].
+DUST2_HD double binomial(rng_state& rng, double n, double p) {
+  if (!(n >= 0) || !math::is_finite(n) || !(p >= 0) || !(p <= 1)) {
+    set_error(rng, ERR_BINOMIAL_INVALID, n, p);
+    return math::quiet_nan();
+  }
+  if (rng.deterministic) {
+    return n * p;
+  }
+  if (n == 0 || p == 0) {
+    return 0;
+  }
+  if (p == 1) {
+    return n;
+  }
+  const bool flip = p > 0.5;
+  const double pp = flip ? 1.0 - p : p;
+  const double x = (n * pp < 10) ? binomial_inversion(rng, n, pp) :
+    binomial_btrs(rng, n, pp);
+  return flip ? n - x : x;
+}
+
+DUST2_HD double poisson_knuth(rng_state& rng, double lambda) {
+  const double enlam = math::exp(-lambda);
+  double prod = 1.0;
+  for (int x = 0; x < MAX_REJECTION_ATTEMPTS; ++x) {
+    prod = prod * random_real(rng);
+    if (prod <= enlam) {
+      return x;
+    }
+  }
+  set_error(rng, ERR_POISSON_INVALID, lambda, 0);
+  return math::quiet_nan();
+}
+
+DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
+  const double slam = std::sqrt(lambda);
+  const double b = 0.931 + 2.53 * slam;
+  const double a = -0.059 + 0.02483 * b;
+  const double vr = 0.9277 - 3.6224 / (b - 2.0);
+  bool have_setup = false;
+  double log_invalpha = 0, loglam = 0;
+  for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
+    const double u = random_real(rng) - 0.5;
+    const double v = random_real(rng);
+    const double us = 0.5 - std::fabs(u);
+    const double k = std::floor((2.0 * a / us + b) * u + lambda + 0.43);
+    if (us >= 0.07 && v <= vr) {
+      return k;
+    }
+    if (k < 0 || (us < 0.013 && v > us)) {
+      continue;
+    }
+    if (!have_setup) {
+      log_invalpha = math::log(1.1239 + 1.1328 / (b - 3.4));
+      loglam = math::log(lambda);
+      have_setup = true;
+    }
+    if (math::log(v) + log_invalpha - math::log(a / (us * us) + b) <=
+        -lambda + k * loglam - math::log_factorial(k)) {
+      return k;
+    }
+  }
+  set_error(rng, ERR_POISSON_INVALID, lambda, 0);
+  return math::quiet_nan();
+}
+
+DUST2_HD double poisson(rng_state& rng, double lambda) {
+  if (!(lambda >= 0) || !math::is_finite(lambda)) {
+    set_error(rng, ERR_POISSON_INVALID, lambda, 0);
+    return math::quiet_nan();
+  }
+  if (rng.deterministic) {
+    return lambda;
+  }
+  if (lambda == 0) {
+    return 0;
+  }
+  return lambda < 10 ? poisson_knuth(rng, lambda) : poisson_ptrs(rng, lambda);
+}
+
+DUST2_HD double exponential_rate(rng_state& rng, double rate) {
+  if (rng.deterministic) {
+    return 1.0 / rate;
+  }
+  return -math::log(1.0 - random_real(rng)) / rate;
+}
+
+DUST2_HD double uniform(rng_state& rng, double min, double max) {
+  if (rng.deterministic) {
+    return 0.5 * (min + max);
+  }
+  return min + (max - min) * random_real(rng);
+}
+
+DUST2_HD double normal(rng_state& rng, double mean, double sd) {
+  if (rng.deterministic) {
+    return mean;
+  }
+  const double u1 = 1.0 - random_real(rng);  // (0, 1]
+  const double u2 = random_real(rng);
+  double s, c;
+  math::sincos_2pi(u2, &s, &c);
+  const double z = std::sqrt(-2.0 * math::log(u1)) * c;
+  return mean + sd * z;
+}
+
+}  // namespace random
+
+namespace density {
+
+// log Poisson(x | lambda), with 0 log 0 = 0.
+DUST2_HD double poisson(double x, double lambda, bool log) {
+  double ret;
+  if (x == 0 && lambda == 0) {
+    ret = 0;
+  } else {
+    ret = x * math::log(lambda) - lambda - math::lgamma(x + 1.0);
+  }
+  return log ? ret : math::exp(ret);
+}
+
+// log NegBinomial(x | size, mu), mean/size parameterisation.
+DUST2_HD double negative_binomial_mu(double x, double size, double mu,
+                                     bool log) {
+  double ret;
+  if (x == 0 && mu == 0) {
+    ret = 0;
+  } else {
+    const double lsm = math::log(size + mu);
+    ret = math::lgamma(x + size) - math::lgamma(size) -
+      math::lgamma(x + 1.0) + size * (math::log(size) - lsm) +
+      x * (math::log(mu) - lsm);
+  }
+  return log ? ret : math::exp(ret);
+}
+
+DUST2_HD double normal(double x, double mu, double sd, bool log) {
+  const double z = (x - mu) / sd;
+  const double ret = -0.5 * z * z - math::log(sd) - math::HALF_LOG_2PI;
+  return log ? ret : math::exp(ret);
+}
+
+}  // namespace density
+}  // namespace dust2gpu

@@ -1,0 +1,124 @@
+// Type-erased interfaces between the C ABI and the templated engines.
+// One object of each kind exists per allocated system / filter handle;
+// the C ABI (capi.cu) owns them and turns C++ exceptions into status
+// codes.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../dust2gpu/common.hpp"
+#include "../dust2gpu/system.hpp"
+
+namespace dust2gpu {
+namespace engine {
+
+// Summary of per-particle errors in the format of
+// inst/include/dust2/errors.hpp:29-54.
+std::string format_errors(const std::vector<particle_error>& errors,
+                          const char* title = "particles",
+                          std::size_t n_max = 4);
+std::string describe_error(const particle_error& e);
+
+struct ode_control {
+  // inst/include/dust2/continuous/control.hpp:11-27; step_size_min is
+  // clamped below by machine epsilon as in
+  // inst/include/dust2/r/continuous/control.hpp:15-17.
+  int max_steps = 10000;
+  double atol = 1e-6;
+  double rtol = 1e-6;
+  double step_size_min = 1e-8;
+  double step_size_max = 1.0 / 0.0;
+  double factor_safe = 0.9;
+  double factor_min = 0.2;
+  double factor_max = 10.0;
+  double beta = 0.04;
+  double constant = 0.2 - 0.04 * 0.75;
+  std::vector<double> critical_times;
+  bool debug_record_step_times = false;
+};
+
+// Per-particle solver statistics (dust_system_internals, R/interface.R).
+struct ode_internals_row {
+  double step_size;
+  double error;
+  long n_steps;
+  long n_steps_accepted;
+  long n_steps_rejected;
+};
+
+class system_api {
+public:
+  virtual ~system_api() = default;
+
+  virtual const char* name() const = 0;
+  virtual bool is_continuous() const = 0;
+  virtual bool has_compare() const = 0;
+  virtual int n_state() const = 0;
+  virtual int n_groups() const = 0;
+  virtual int n_particles_total() const = 0;
+  virtual const std::vector<int>& n_particles() const = 0;
+  virtual std::vector<packing_entry> packing_state() const = 0;
+
+  virtual double time() const = 0;
+  virtual double dt() const = 0;
+  virtual void set_time(double time) = 0;
+
+  virtual void run_to_time(double time) = 0;
+  virtual void set_state_initial() = 0;
+  // Full state in dust2's dimension order: state fastest, then particle,
+  // then group.
+  virtual void get_state(double* out) = 0;
+  virtual void put_state(const double* in) = 0;
+  // Raw generator state: 4 words per stream, streams in particle order.
+  virtual void get_rng_state(std::uint64_t* out) = 0;
+  virtual void put_rng_state(const std::uint64_t* in) = 0;
+  virtual int n_pars() const = 0;
+  virtual void update_pars(const double* pars, const int* index_group,
+                           int n_index_group) = 0;
+  // out: [time][group][particle][index_state or all state]
+  virtual void simulate(const double* times, int n_times,
+                        const int* index_state, int n_index_state,
+                        double* out) = 0;
+  // index: group-local particle index per particle, group-major
+  virtual void reorder(const int* index) = 0;
+  // data: [group][n_data] doubles; out: [group][particle]
+  virtual int n_data() const = 0;
+  virtual void compare_data(const double* data, int n_groups_data,
+                            double* out) = 0;
+  virtual bool errors_pending() const = 0;
+  virtual std::vector<ode_internals_row> ode_internals() = 0;
+  virtual std::vector<std::vector<double>> ode_step_times() = 0;
+};
+
+class filter_api {
+public:
+  virtual ~filter_api() = default;
+  virtual system_api& sys() = 0;
+  virtual int n_times() const = 0;
+  // initial: optional full state (dust2 order) applied instead of the
+  // system's initial conditions; index_group: groups to run (nullptr =
+  // all).  ll_out receives one value per requested group.
+  virtual void run(const double* initial, const int* index_group,
+                   int n_index_group, double* ll_out) = 0;
+  virtual void update_pars(const double* pars, const int* index_group,
+                           int n_index_group) = 0;
+  // Raw generator state in the layout of
+  // inst/include/dust2/r/filter.hpp:273-298: per group, the 2 filter
+  // streams followed by that group's particle streams.
+  virtual void get_rng_state(std::uint64_t* out) = 0;
+  virtual void put_rng_state(const std::uint64_t* in) = 0;
+  virtual std::size_t n_rng_streams() const = 0;
+  // For each group, draw (once per run) a random particle from the
+  // group's second filter stream (filter.hpp:130-138).
+  virtual std::vector<int> select_random_particle() = 0;
+  virtual bool has_run() const = 0;
+  // Fallback statistics of the resampler: groups recomputed serially.
+  virtual long n_serial_fallbacks() const = 0;
+  // Run options.
+  virtual void set_use_graph(bool use) = 0;
+};
+
+}  // namespace engine
+}  // namespace dust2gpu

@@ -1,0 +1,119 @@
+// Per-system factory: builds shared state from the flat parameter table,
+// data from the flat data table, and the device engine.  Each system's
+// translation unit (systems_*.cu) instantiates this once and registers
+// it at load time.
+#pragma once
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "continuous.cuh"
+#include "discrete.cuh"
+#include "filter.cuh"
+#include "registry.hpp"
+
+namespace dust2gpu {
+namespace engine {
+
+template <typename T>
+std::vector<typename T::shared_state> build_shared_groups(const double* pars,
+                                                          int n_groups) {
+  const int np = parameter_length<T>();
+  std::vector<typename T::shared_state> shared;
+  shared.reserve(n_groups);
+  int n_state = -1;
+  for (int g = 0; g < n_groups; ++g) {
+    shared.push_back(T::build_shared(pars + static_cast<std::size_t>(g) * np));
+    const int n_g = T::n_state(shared.back());
+    // inst/include/dust2/r/helpers.hpp:333-369
+    if (g > 0 && n_g != n_state) {
+      throw std::runtime_error(
+        "State length for group " + std::to_string(g + 1) +
+        " was different to previous groups; total length was expected to "
+        "be " + std::to_string(n_state) + " but it was " +
+        std::to_string(n_g));
+    }
+    n_state = n_g;
+  }
+  return shared;
+}
+
+template <typename T>
+system_api* create_system(const double* pars, int n_groups,
+                          const std::vector<int>& n_particles, double time,
+                          double dt, const ode_control& control,
+                          const std::vector<std::uint64_t>& rng_words,
+                          bool deterministic, int tile_size) {
+  auto shared = build_shared_groups<T>(pars, n_groups);
+  if constexpr (is_continuous<T>()) {
+    return new continuous_system<T>(std::move(shared), time, control,
+                                    n_particles, rng_words, deterministic,
+                                    tile_size);
+  } else {
+    return new discrete_system<T>(std::move(shared), time, dt, n_particles,
+                                  rng_words, deterministic, tile_size);
+  }
+}
+
+template <typename T>
+filter_api* create_filter(const double* pars, int n_groups,
+                          const std::vector<int>& n_particles,
+                          double time_start, const double* times, int n_times,
+                          const double* data, int n_groups_data, double dt,
+                          const std::vector<std::uint64_t>& rng_words,
+                          int tile_size) {
+  if constexpr (is_continuous<T>() || !has_compare_data<T>::value) {
+    throw std::runtime_error(
+      is_continuous<T>() ?
+      "Can't use 'dust_filter_create()' with continuous-time models" :
+      std::string("Can't create filter; the '") + T::name +
+      "' system does not have 'compare_data' support");
+  } else {
+    auto shared = build_shared_groups<T>(pars, n_groups);
+    // Split the stream block (r/discrete/filter.hpp:63-75): per group the
+    // first 2 streams go to the filter, the rest to the particles.
+    std::vector<std::uint64_t> sys_words;
+    std::size_t pos = 0;
+    for (int g = 0; g < n_groups; ++g) {
+      pos += 8;
+      for (int w = 0; w < 4 * n_particles[g]; ++w) {
+        sys_words.push_back(rng_words[pos++]);
+      }
+    }
+    auto sys = std::make_unique<discrete_system<T>>(
+      std::move(shared), time_start, dt, n_particles, sys_words, false,
+      tile_size);
+    const int nd = sys->n_data();
+    std::vector<typename T::data_type> d;
+    d.reserve(static_cast<std::size_t>(n_times) * n_groups_data);
+    for (int i = 0; i < n_times * n_groups_data; ++i) {
+      d.push_back(T::build_data(data + static_cast<std::size_t>(i) * nd));
+    }
+    std::vector<double> t(times, times + n_times);
+    return new filter_engine<T>(std::move(sys), time_start, std::move(t),
+                                std::move(d), n_groups_data, rng_words);
+  }
+}
+
+template <typename T>
+struct registrar {
+  system_factory factory;
+  explicit registrar() {
+    factory.name = T::name;
+    factory.continuous = is_continuous<T>();
+    factory.has_compare = has_compare_data<T>::value;
+    factory.info_json = &system_info_json<T>;
+    factory.create_system = &create_system<T>;
+    factory.create_filter = &create_filter<T>;
+    register_system(&factory);
+  }
+};
+
+}  // namespace engine
+}  // namespace dust2gpu
+
+// One system per translation unit.
+#define DUST2_REGISTER_SYSTEM(T)                                          \
+  static ::dust2gpu::engine::registrar<T> dust2_registrar_instance

@@ -1,0 +1,528 @@
+// Bootstrap particle filter on the GPU: the counterpart of dust2::filter
+// (inst/include/dust2/filter.hpp:11-176) and its helpers
+// scale_log_weights / resample_weight (filter_details.hpp:11-74).
+//
+// Per data time, for the groups being run:
+//   1. k_step_compare  one thread per particle: advance the particle to
+//                      the data time (filter.hpp:59), evaluate
+//                      compare_data (:60), and reduce per group the
+//                      "any weight non-zero" flag (:71-72) and the maximum
+//                      log weight (filter_details.hpp:19-25; NaN counts as
+//                      -Inf).
+//   2. k_weights       one block per tile: w = exp(logw - max) and the
+//                      tile's inclusive prefix sums (FP64).
+//   3. k_group         one warp per group: scan of tile totals, the
+//                      log-likelihood increment log(sum/n) + max (:32-38),
+//                      and the uniform u from the group's filter stream 2g
+//                      (filter.hpp:75).
+//   4. k_resample      one thread per particle: systematic resampling
+//                      target uu_i = sum*u/n + i*sum/n and a search of the
+//                      prefix sums (filter_details.hpp:45-74).
+//   5. k_fallback      one warp per flagged group: the serial algorithm.
+//   6. k_reorder       gather of the resampled state (discrete/system.hpp
+//                      :170-181).
+//
+// Exactness of the resampling indices.  dust2 accumulates the weights
+// serially; a parallel scan rounds differently, so a search target that
+// falls within a few ulps of a cumulative boundary could pick a
+// neighbouring particle.  Step 4 therefore checks every decision against
+// a rigorous error bound: the serial and parallel prefix sums of n
+// non-negative weights (each within 2 ulp of the other side's exp) differ
+// by at most (n + log2 n + 6) u sum (u = 2^-53), and the targets, computed
+// from either total, by at most that plus 8 u sum.  A decision is accepted
+// only when both neighbouring prefix sums are farther than
+// (4n + 128) u sum from the target; otherwise the whole group is recomputed
+// serially (step 5), which is the reference algorithm verbatim.  The
+// log-likelihood uses the parallel total; it matches the serial one to
+// better than n u relative.
+//
+// The whole sequence for all data times is captured once into a CUDA
+// graph and replayed on every run.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "../dust2gpu/math.hpp"
+#include "../dust2gpu/random.hpp"
+#include "api.hpp"
+#include "device.cuh"
+#include "discrete.cuh"
+#include "kernels_common.cuh"
+
+namespace dust2gpu {
+namespace engine {
+
+enum group_mode : int {
+  MODE_KEEP = 0,      // no data: particles stay where they are
+  MODE_RESAMPLE = 1,  // systematic resampling by weight
+  MODE_FIRST = 2      // every particle takes particle 0 (n == 1 or all -Inf)
+};
+
+// Per-group scratch of the filter, all device pointers.
+struct filter_view {
+  const tile* tiles;
+  const int* active;          // [n_groups] 1 = run this group
+  const int* n_particles;     // [n_groups]
+  const int* offset;          // [n_groups]
+  const int* tile_first;      // [n_groups]
+  const int* tile_count;      // [n_groups]
+  double* w;                  // [n_total] raw log weights
+  double* ew;                 // [n_total] exp(w - max)
+  double* pre;                // [n_total] tile-local inclusive prefix
+  double* tile_sum;           // [n_tiles]
+  double* tile_off;           // [n_tiles] exclusive offsets within group
+  unsigned long long* gkey;   // [n_groups] ordered key of max log weight
+  int* gnz;                   // [n_groups] any weight != 0
+  int* gflag;                 // [n_groups] ambiguous decision seen
+  int* mode;                  // [n_groups] group_mode
+  double* ll;                 // [n_groups]
+  double* gu;                 // [n_groups] uniform draw
+  double* guu0;               // [n_groups]
+  double* gdu;                // [n_groups]
+  double* gtot;               // [n_groups]
+  int* idx;                   // [n_total] group-local source particle
+  std::uint64_t* frng;        // [2 n_groups][4] filter streams
+  int* set_initial;           // scalar flag read by the initial kernel
+};
+
+__global__ void k_filter_reset(filter_view f, int n_groups);
+
+template <typename T>
+__global__ void k_initial_flagged(system_view<T> v, const int* flag,
+                                  double time) {
+  __shared__ shared_smem<T> sm;
+  if (*flag == 0) {
+    return;
+  }
+  const tile tl = v.tiles[blockIdx.x];
+  sm.load(v, tl.group);
+  __syncthreads();
+  if (static_cast<int>(threadIdx.x) >= tl.count) {
+    return;
+  }
+  const int k = tl.start + threadIdx.x;
+  auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
+  typename T::internal_state internal{};
+  double x[T::n_state_max];
+  load_state<T>(v, k, x);
+  T::initial(time, sm.shared(), internal, rng, x);
+  store_state<T>(v, k, x);
+  store_rng(v.rng, v.stride, k, rng);
+  capture_error(v.errors, v.any_error, k, rng);
+}
+
+template <typename T>
+__global__ void k_step_compare(system_view<T> v, filter_view f, double time,
+                               double dt, int n_steps, double time_compare,
+                               const typename T::data_type* data,
+                               int n_groups_data) {
+  __shared__ shared_smem<T> sm;
+  __shared__ double red[33];
+  const tile tl = v.tiles[blockIdx.x];
+  if (!f.active[tl.group]) {
+    return;
+  }
+  sm.load(v, tl.group);
+  __syncthreads();
+  const bool valid = static_cast<int>(threadIdx.x) < tl.count;
+  double logw = 0;
+  if (valid) {
+    const int k = tl.start + threadIdx.x;
+    auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
+    typename T::internal_state internal{};
+    double x[T::n_state_max];
+    double y[T::n_state_max];
+    load_state<T>(v, k, x);
+    run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero, rng,
+                    x, y);
+    const auto& d = data[n_groups_data == 1 ? 0 : tl.group];
+    logw = T::compare_data(time_compare, x, d, sm.shared(), internal, rng);
+    store_state<T>(v, k, x);
+    store_rng(v.rng, v.stride, k, rng);
+    capture_error(v.errors, v.any_error, k, rng);
+    f.w[k] = logw;
+  }
+  // NaN != 0 counts as data (filter.hpp:71-72); NaN is -Inf for the max.
+  const int nz = __syncthreads_or(valid && logw != 0);
+  const double mx = block_max(valid && !(logw != logw) ? logw : -INFINITY,
+                              red);
+  if (threadIdx.x == 0) {
+    if (nz) {
+      atomicOr(f.gnz + tl.group, 1);
+    }
+    atomicMax(f.gkey + tl.group, ordered_key(mx));
+  }
+}
+
+__global__ void k_weights(filter_view f);
+__global__ void k_group(filter_view f, int n_groups);
+__global__ void k_resample(filter_view f);
+__global__ void k_fallback(filter_view f);
+
+// Host-side description of the observation schedule.
+struct obs_step {
+  double t0;            // system time before the step
+  int n_steps;
+  double t_compare;     // system time after the step
+};
+
+template <typename T>
+class filter_engine : public filter_api {
+public:
+  using data_type = typename T::data_type;
+
+  // data: [n_times][n_groups_data] data_type; rng_words: the full stream
+  // block of the filter, per group [2 filter | n_g particle] streams.
+  filter_engine(std::unique_ptr<discrete_system<T>> sys, double time_start,
+                std::vector<double> times, std::vector<data_type> data,
+                int n_groups_data, const std::vector<std::uint64_t>& rng_words) :
+    sys_(std::move(sys)), time_start_(time_start), times_(std::move(times)),
+    n_groups_data_(n_groups_data) {
+    const auto& L = sys_->layout();
+    const int G = L.n_groups;
+    const int N = L.n_total;
+    const int NT = L.n_tiles();
+    // schedule
+    double t = time_start_;
+    for (double ti : times_) {
+      const int n = static_cast<int>(
+        std::round(std::max(0.0, ti - t) / sys_->dt()));
+      schedule_.push_back(obs_step{t, n, t + n * sys_->dt()});
+      t = t + n * sys_->dt();
+    }
+    active_.resize(G);
+    n_part_.resize(G);
+    offset_.resize(G);
+    tile_first_.resize(G);
+    tile_count_.resize(G);
+    w_.resize(N);
+    ew_.resize(N);
+    pre_.resize(N);
+    tile_sum_.resize(NT);
+    tile_off_.resize(NT);
+    gkey_.resize(G);
+    gnz_.resize(G);
+    gflag_.resize(G);
+    mode_.resize(G);
+    ll_.resize(G);
+    gu_.resize(G);
+    guu0_.resize(G);
+    gdu_.resize(G);
+    gtot_.resize(G);
+    idx_.resize(N);
+    frng_.resize(8 * static_cast<std::size_t>(G));
+    set_initial_.resize(1);
+    data_.resize(data.size());
+    auto s = sys_->stream();
+    DUST2_CUDA(cudaMemcpyAsync(n_part_.data(), L.n_particles.data(),
+                               G * sizeof(int), cudaMemcpyHostToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(offset_.data(), L.offset.data(),
+                               G * sizeof(int), cudaMemcpyHostToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(tile_first_.data(), L.tile_first.data(),
+                               G * sizeof(int), cudaMemcpyHostToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(tile_count_.data(), L.tile_count.data(),
+                               G * sizeof(int), cudaMemcpyHostToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(data_.data(), data.data(),
+                               data.size() * sizeof(data_type),
+                               cudaMemcpyHostToDevice, s));
+    put_rng_state(rng_words.data());
+    sys_->sync();
+  }
+
+  system_api& sys() override {
+    return *sys_;
+  }
+  discrete_system<T>& system() {
+    return *sys_;
+  }
+  int n_times() const override {
+    return static_cast<int>(times_.size());
+  }
+  bool has_run() const override {
+    return has_run_;
+  }
+  long n_serial_fallbacks() const override {
+    return n_fallbacks_;
+  }
+  void set_use_graph(bool use) override {
+    use_graph_ = use;
+  }
+
+  filter_view view() {
+    const auto& L = sys_->layout();
+    (void)L;
+    return filter_view{sys_->tiles_dev(), active_.data(), n_part_.data(),
+                       offset_.data(), tile_first_.data(),
+                       tile_count_.data(), w_.data(), ew_.data(), pre_.data(),
+                       tile_sum_.data(), tile_off_.data(), gkey_.data(),
+                       gnz_.data(), gflag_.data(), mode_.data(), ll_.data(),
+                       gu_.data(), guu0_.data(), gdu_.data(), gtot_.data(),
+                       idx_.data(), frng_.data(), set_initial_.data()};
+  }
+
+  void run(const double* initial, const int* index_group, int n_index_group,
+           double* ll_out) override {
+    auto& S = *sys_;
+    const auto& L = S.layout();
+    const int G = L.n_groups;
+    auto s = S.stream();
+    std::vector<int> active(G, index_group == nullptr ? 1 : 0);
+    if (index_group != nullptr) {
+      for (int i = 0; i < n_index_group; ++i) {
+        active[index_group[i]] = 1;
+      }
+    }
+    // reset(): errors, time and (optionally) state (filter.hpp:156-175)
+    S.reset_errors();
+    S.set_time(time_start_);
+    if (initial != nullptr) {
+      S.put_state(initial);
+    }
+    const int set_initial = initial == nullptr ? 1 : 0;
+    DUST2_CUDA(cudaMemcpyAsync(active_.data(), active.data(), G * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(set_initial_.data(), &set_initial,
+                               sizeof(int), cudaMemcpyHostToDevice, s));
+    if (use_graph_) {
+      if (graph_exec_ == nullptr || graph_state_ptr_ != S.state_ptr()) {
+        capture();
+      }
+      DUST2_CUDA(cudaGraphLaunch(graph_exec_, s));
+    } else {
+      enqueue();
+    }
+    std::vector<double> ll(G);
+    DUST2_CUDA(cudaMemcpyAsync(ll.data(), ll_.data(), G * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    std::vector<int> flags(G);
+    DUST2_CUDA(cudaMemcpyAsync(flags.data(), fallback_count_.data(),
+                               G * sizeof(int), cudaMemcpyDeviceToHost, s));
+    S.check_errors_after();
+    for (int g = 0; g < G; ++g) {
+      n_fallbacks_ += flags[g];
+    }
+    S.set_time(schedule_.empty() ? time_start_ : schedule_.back().t_compare);
+    if (index_group == nullptr) {
+      for (int g = 0; g < G; ++g) {
+        ll_out[g] = ll[g];
+      }
+    } else {
+      for (int i = 0; i < n_index_group; ++i) {
+        ll_out[i] = ll[index_group[i]];
+      }
+    }
+    random_particle_.assign(G, -1);
+    has_run_ = true;
+  }
+
+  void update_pars(const double* pars, const int* index_group,
+                   int n_index_group) override {
+    sys_->update_pars(pars, index_group, n_index_group);
+  }
+
+  std::size_t n_rng_streams() const override {
+    const auto& L = sys_->layout();
+    return static_cast<std::size_t>(L.n_total) + 2 * L.n_groups;
+  }
+
+  void get_rng_state(std::uint64_t* out) override {
+    const auto& L = sys_->layout();
+    const int G = L.n_groups;
+    std::vector<std::uint64_t> f(8 * static_cast<std::size_t>(G));
+    DUST2_CUDA(cudaMemcpy(f.data(), frng_.data(), f.size() * 8,
+                          cudaMemcpyDeviceToHost));
+    std::vector<std::uint64_t> p(4 * static_cast<std::size_t>(L.n_total));
+    sys_->get_rng_state(p.data());
+    std::size_t pos = 0;
+    for (int g = 0; g < G; ++g) {
+      for (int w = 0; w < 8; ++w) {
+        out[pos++] = f[8 * g + w];
+      }
+      const std::size_t from = 4 * static_cast<std::size_t>(L.offset[g]);
+      for (std::size_t w = 0; w < 4 * static_cast<std::size_t>(
+             L.n_particles[g]); ++w) {
+        out[pos++] = p[from + w];
+      }
+    }
+  }
+
+  void put_rng_state(const std::uint64_t* in) override {
+    const auto& L = sys_->layout();
+    const int G = L.n_groups;
+    std::vector<std::uint64_t> f(8 * static_cast<std::size_t>(G));
+    std::vector<std::uint64_t> p(4 * static_cast<std::size_t>(L.n_total));
+    std::size_t pos = 0;
+    for (int g = 0; g < G; ++g) {
+      for (int w = 0; w < 8; ++w) {
+        f[8 * g + w] = in[pos++];
+      }
+      const std::size_t to = 4 * static_cast<std::size_t>(L.offset[g]);
+      for (std::size_t w = 0; w < 4 * static_cast<std::size_t>(
+             L.n_particles[g]); ++w) {
+        p[to + w] = in[pos++];
+      }
+    }
+    DUST2_CUDA(cudaMemcpy(frng_.data(), f.data(), f.size() * 8,
+                          cudaMemcpyHostToDevice));
+    sys_->put_rng_state(p.data());
+  }
+
+  std::vector<int> select_random_particle() override {
+    const auto& L = sys_->layout();
+    const int G = L.n_groups;
+    if (static_cast<int>(random_particle_.size()) != G) {
+      random_particle_.assign(G, -1);
+    }
+    bool any = false;
+    for (int g = 0; g < G; ++g) {
+      any = any || random_particle_[g] < 0;
+    }
+    if (any) {
+      std::vector<std::uint64_t> f(8 * static_cast<std::size_t>(G));
+      DUST2_CUDA(cudaMemcpy(f.data(), frng_.data(), f.size() * 8,
+                            cudaMemcpyDeviceToHost));
+      for (int g = 0; g < G; ++g) {
+        if (random_particle_[g] < 0) {
+          random::rng_state r{};
+          for (int w = 0; w < 4; ++w) {
+            r.state[w] = f[8 * g + 4 + w];
+          }
+          const double u = random::random_real(r);
+          random_particle_[g] =
+            static_cast<int>(std::floor(u * L.n_particles[g]));
+          for (int w = 0; w < 4; ++w) {
+            f[8 * g + 4 + w] = r.state[w];
+          }
+        }
+      }
+      DUST2_CUDA(cudaMemcpy(frng_.data(), f.data(), f.size() * 8,
+                            cudaMemcpyHostToDevice));
+    }
+    return random_particle_;
+  }
+
+  ~filter_engine() override {
+    if (graph_exec_ != nullptr) {
+      cudaGraphExecDestroy(graph_exec_);
+    }
+    if (graph_ != nullptr) {
+      cudaGraphDestroy(graph_);
+    }
+  }
+
+private:
+  // The launch sequence of one run; captured into a graph or issued
+  // directly.
+  void enqueue() {
+    auto& S = *sys_;
+    const auto& L = S.layout();
+    auto s = S.stream();
+    const int G = L.n_groups;
+    const int NT = L.n_tiles();
+    const int TS = L.tile_size;
+    if (fallback_count_.size() != static_cast<std::size_t>(G)) {
+      fallback_count_.resize(G);
+    }
+    filter_view f = view();
+    f.gflag = gflag_.data();
+    k_filter_reset<<<n_blocks(G, 128), 128, 0, s>>>(f, G);
+    DUST2_CUDA(cudaMemsetAsync(fallback_count_.data(), 0, G * sizeof(int), s));
+    system_view<T> v = S.view();
+    k_initial_flagged<T><<<NT, TS, 0, s>>>(v, set_initial_.data(),
+                                           time_start_);
+    double* cur = S.state_ptr();
+    double* other = S.state_other_ptr();
+    for (std::size_t i = 0; i < schedule_.size(); ++i) {
+      const auto& st = schedule_[i];
+      v.state = cur;
+      k_step_compare<T><<<NT, TS, 0, s>>>(
+        v, f, st.t0, S.dt(), st.n_steps, st.t_compare,
+        data_.data() + i * n_groups_data_, n_groups_data_);
+      k_weights<<<NT, TS, 0, s>>>(f);
+      k_group<<<G, 32, 0, s>>>(f, G);
+      k_resample<<<NT, TS, 0, s>>>(f);
+      k_fallback_counted(f, s);
+      k_reorder<<<NT, TS, 0, s>>>(cur, other, L.stride, S.n_state(),
+                                  L.tiles.empty() ? nullptr : S.tiles_dev(),
+                                  offset_.data(), idx_.data(), mode_.data());
+      std::swap(cur, other);
+    }
+    if (cur != S.state_ptr()) {
+      DUST2_CUDA(cudaMemcpyAsync(S.state_ptr(), cur,
+                                 static_cast<std::size_t>(S.n_state()) *
+                                 L.stride * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
+    }
+    DUST2_CUDA(cudaGetLastError());
+  }
+
+  void k_fallback_counted(filter_view f, cudaStream_t s);
+
+  void capture() {
+    auto s = sys_->stream();
+    if (graph_exec_ != nullptr) {
+      cudaGraphExecDestroy(graph_exec_);
+      graph_exec_ = nullptr;
+    }
+    if (graph_ != nullptr) {
+      cudaGraphDestroy(graph_);
+      graph_ = nullptr;
+    }
+    DUST2_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue();
+    } catch (...) {
+      cudaGraph_t g;
+      cudaStreamEndCapture(s, &g);
+      if (g != nullptr) {
+        cudaGraphDestroy(g);
+      }
+      throw;
+    }
+    DUST2_CUDA(cudaStreamEndCapture(s, &graph_));
+    DUST2_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+    graph_state_ptr_ = sys_->state_ptr();
+  }
+
+  std::unique_ptr<discrete_system<T>> sys_;
+  double time_start_;
+  std::vector<double> times_;
+  int n_groups_data_;
+  std::vector<obs_step> schedule_;
+  std::vector<int> random_particle_;
+  bool has_run_ = false;
+  bool use_graph_ = true;
+  long n_fallbacks_ = 0;
+
+  device_array<int> active_, n_part_, offset_, tile_first_, tile_count_;
+  device_array<double> w_, ew_, pre_, tile_sum_, tile_off_;
+  device_array<unsigned long long> gkey_;
+  device_array<int> gnz_, gflag_, mode_;
+  device_array<double> ll_, gu_, guu0_, gdu_, gtot_;
+  device_array<int> idx_;
+  device_array<std::uint64_t> frng_;
+  device_array<int> set_initial_;
+  device_array<int> fallback_count_;
+  device_array<data_type> data_;
+
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  const double* graph_state_ptr_ = nullptr;
+};
+
+// Serial fallback, counting how many groups needed it.
+__global__ void k_fallback_count(filter_view f, int* count);
+
+template <typename T>
+void filter_engine<T>::k_fallback_counted(filter_view f, cudaStream_t s) {
+  const int G = sys_->layout().n_groups;
+  k_fallback_count<<<G, 32, 0, s>>>(f, fallback_count_.data());
+}
+
+}  // namespace engine
+}  // namespace dust2gpu

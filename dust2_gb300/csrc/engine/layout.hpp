@@ -1,0 +1,83 @@
+// How particles of (possibly uneven) parameter groups are laid out in
+// device memory, and how they are cut into tiles of one CUDA block each.
+//
+// dust2 stores state particle-major, `state_[(n_particles*g + j)*n_state
+// + s]` (inst/include/dust2/discrete/system.hpp:72-73), with the same
+// number of particles in every group.  Here state is structure-of-arrays,
+// `state[s * stride + k]` with k the global particle index (group-major),
+// so that consecutive threads touch consecutive addresses; groups may have
+// different particle counts (the batched workloads need that), and a tile
+// never straddles two groups, so a block loads its group's parameters
+// once into shared memory and reduces over its group with block-wide
+// primitives.
+#pragma once
+
+#include <stdexcept>
+#include <vector>
+
+namespace dust2gpu {
+namespace engine {
+
+struct tile {
+  int group;  // parameter group of every particle in the tile
+  int start;  // global index of the first particle
+  int count;  // particles in the tile (<= tile size)
+  int local;  // index of the first particle within its group
+};
+
+struct group_layout {
+  std::vector<int> n_particles;  // per group
+  std::vector<int> offset;       // global index of a group's first particle
+  std::vector<int> tile_first;   // first tile of each group
+  std::vector<int> tile_count;   // tiles in each group
+  std::vector<tile> tiles;
+  int n_groups = 0;
+  int n_total = 0;
+  int stride = 0;                // SoA stride, a multiple of 32
+  int tile_size = 0;
+  bool uniform = true;           // all groups have the same particle count
+
+  group_layout() = default;
+
+  group_layout(const std::vector<int>& n, int tile_size_) :
+    n_particles(n), tile_size(tile_size_) {
+    if (n.empty()) {
+      throw std::runtime_error("Expected at least one group");
+    }
+    if (tile_size <= 0 || tile_size % 32 != 0 || tile_size > 1024) {
+      throw std::runtime_error("tile size must be a multiple of 32 <= 1024");
+    }
+    n_groups = static_cast<int>(n.size());
+    long total = 0;
+    for (int g = 0; g < n_groups; ++g) {
+      if (n[g] < 1) {
+        throw std::runtime_error("'n_particles' must be at least 1");
+      }
+      if (n[g] != n[0]) {
+        uniform = false;
+      }
+      offset.push_back(static_cast<int>(total));
+      tile_first.push_back(static_cast<int>(tiles.size()));
+      const int nt = (n[g] + tile_size - 1) / tile_size;
+      tile_count.push_back(nt);
+      for (int t = 0; t < nt; ++t) {
+        const int local = t * tile_size;
+        const int count = std::min(tile_size, n[g] - local);
+        tiles.push_back(tile{g, static_cast<int>(total) + local, count, local});
+      }
+      total += n[g];
+      if (total > (1L << 30)) {
+        throw std::runtime_error("too many particles");
+      }
+    }
+    n_total = static_cast<int>(total);
+    stride = ((n_total + 31) / 32) * 32;
+  }
+
+  int n_tiles() const {
+    return static_cast<int>(tiles.size());
+  }
+};
+
+}  // namespace engine
+}  // namespace dust2gpu

@@ -1,0 +1,230 @@
+// System-independent kernels of the particle filter: weight
+// normalisation, per-group log-sum-exp and resampling (see
+// engine/filter.cuh for the algorithm and its exactness argument).
+#include <cfloat>
+#include <cmath>
+
+#include "dust2gpu/math.hpp"
+#include "dust2gpu/random.hpp"
+#include "engine/device.cuh"
+#include "engine/filter.cuh"
+
+namespace dust2gpu {
+namespace engine {
+
+__global__ void k_filter_reset(filter_view f, int n_groups) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_groups) {
+    return;
+  }
+  f.ll[g] = 0;
+  f.gkey[g] = ordered_key(-INFINITY);
+  f.gnz[g] = 0;
+  f.gflag[g] = 0;
+  f.mode[g] = MODE_KEEP;
+}
+
+// exp(w - max) and tile-local inclusive prefix sums.
+__global__ void k_weights(filter_view f) {
+  __shared__ double smem[33];
+  const tile tl = f.tiles[blockIdx.x];
+  const int g = tl.group;
+  if (!f.active[g] || !f.gnz[g] || f.n_particles[g] == 1) {
+    return;
+  }
+  const double mx = ordered_value(f.gkey[g]);
+  if (mx == -INFINITY) {
+    return;
+  }
+  const bool valid = static_cast<int>(threadIdx.x) < tl.count;
+  const int k = tl.start + threadIdx.x;
+  double e = 0;
+  if (valid) {
+    const double w = f.w[k];
+    e = (w != w) ? 0.0 : math::exp(w - mx);
+  }
+  double total;
+  const double incl = block_inclusive_scan(e, smem, &total);
+  if (valid) {
+    f.ew[k] = e;
+    f.pre[k] = incl;
+  }
+  if (threadIdx.x == 0) {
+    f.tile_sum[blockIdx.x] = total;
+  }
+}
+
+// One warp per group: tile offsets, log-likelihood increment and the
+// resampling uniform; then clear the per-observation reductions.
+__global__ void k_group(filter_view f, int n_groups) {
+  const int g = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (g >= n_groups || !f.active[g]) {
+    return;
+  }
+  const int n = f.n_particles[g];
+  const bool nz = f.gnz[g] != 0;
+  const double mx = ordered_value(f.gkey[g]);
+  int mode = MODE_KEEP;
+  double tot = 0;
+  if (nz && n > 1 && mx != -INFINITY) {
+    const int t0 = f.tile_first[g];
+    const int nt = f.tile_count[g];
+    double carry = 0;
+    for (int base = 0; base < nt; base += 32) {
+      const int t = base + lane;
+      const double v = t < nt ? f.tile_sum[t0 + t] : 0.0;
+      const double incl = warp_inclusive_scan(v);
+      if (t < nt) {
+        f.tile_off[t0 + t] = carry + (incl - v);
+      }
+      carry = carry + __shfl_sync(0xffffffffu, incl, 31);
+    }
+    tot = carry;
+  }
+  if (lane == 0) {
+    if (nz) {
+      random::rng_state r{};
+      for (int w = 0; w < 4; ++w) {
+        r.state[w] = f.frng[8 * g + w];
+      }
+      r.deterministic = false;
+      double inc;
+      if (n == 1) {
+        inc = f.w[f.offset[g]];
+        mode = MODE_FIRST;
+      } else if (mx == -INFINITY) {
+        inc = -INFINITY;
+        mode = MODE_FIRST;
+      } else {
+        inc = math::log(tot / n) + mx;
+        mode = MODE_RESAMPLE;
+      }
+      f.ll[g] += inc;
+      const double u = random::random_real(r);
+      for (int w = 0; w < 4; ++w) {
+        f.frng[8 * g + w] = r.state[w];
+      }
+      f.gu[g] = u;
+      f.gtot[g] = tot;
+      f.guu0[g] = tot * u / n;
+      f.gdu[g] = tot / n;
+    }
+    f.mode[g] = mode;
+    f.gkey[g] = ordered_key(-INFINITY);
+    f.gnz[g] = 0;
+    f.gflag[g] = 0;
+  }
+}
+
+// Prefix sum Q_m (weights 0..m of the group) for group-local index m.
+__device__ __forceinline__ double prefix_at(const filter_view& f, int g,
+                                            int m, int tile_size) {
+  const int t = f.tile_first[g] + m / tile_size;
+  return f.tile_off[t] + f.pre[f.offset[g] + m];
+}
+
+__global__ void k_resample(filter_view f) {
+  const tile tl = f.tiles[blockIdx.x];
+  const int g = tl.group;
+  if (!f.active[g]) {
+    return;
+  }
+  const int mode = f.mode[g];
+  if (mode == MODE_KEEP || static_cast<int>(threadIdx.x) >= tl.count) {
+    return;
+  }
+  const int k = tl.start + threadIdx.x;
+  if (mode == MODE_FIRST) {
+    f.idx[k] = 0;
+    return;
+  }
+  const int n = f.n_particles[g];
+  const int ts = blockDim.x;
+  const int i = tl.local + threadIdx.x;
+  const double tot = f.gtot[g];
+  const double uu = f.guu0[g] + static_cast<double>(i) * f.gdu[g];
+  // first tile whose last prefix reaches uu
+  const int t0 = f.tile_first[g];
+  int lo = 0, hi = f.tile_count[g];
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (f.tile_off[t0 + mid] + f.tile_sum[t0 + mid] >= uu) {
+      hi = mid;
+    } else {
+      lo = mid + 1;
+    }
+  }
+  int m;
+  if (lo == f.tile_count[g]) {
+    m = n - 1;  // past the end: the serial loop stops at j == n
+  } else {
+    const int first = lo * ts;
+    const int last = min(n, first + ts) - 1;
+    int a = first, b = last;
+    const double off = f.tile_off[t0 + lo];
+    const double* pre = f.pre + f.offset[g];
+    while (a < b) {
+      const int mid = (a + b) >> 1;
+      if (off + pre[mid] >= uu) {
+        b = mid;
+      } else {
+        a = mid + 1;
+      }
+    }
+    m = a;
+  }
+  // Robustness of the decision against serial-summation rounding.  The
+  // serial loop returns m exactly when its prefix of m weights is below
+  // the target (needed only for m > 0: index 0 results whether the target
+  // is below or inside the first weight) and its prefix of m + 1 weights
+  // reaches it (needed only for m < n - 1: the loop stops at the last
+  // particle anyway).
+  const double margin = (4.0 * n + 128.0) * 0x1.0p-53 * tot;
+  bool ok = true;
+  if (m > 0) {
+    ok = ok && prefix_at(f, g, m - 1, ts) < uu - margin;
+  }
+  if (m < n - 1) {
+    ok = ok && prefix_at(f, g, m, ts) >= uu + margin;
+  }
+  f.idx[k] = m;
+  if (!ok) {
+    atomicOr(f.gflag + g, 1);
+  }
+}
+
+// The reference algorithm verbatim (filter_details.hpp:45-74) for groups
+// with an ambiguous parallel decision.
+__global__ void k_fallback_count(filter_view f, int* count) {
+  const int g = blockIdx.x;
+  if (!f.active[g] || f.mode[g] != MODE_RESAMPLE || !f.gflag[g] ||
+      threadIdx.x != 0) {
+    return;
+  }
+  count[g] += 1;
+  const int n = f.n_particles[g];
+  const double* w = f.ew + f.offset[g];
+  int* idx = f.idx + f.offset[g];
+  double tot = 0;
+  for (int j = 0; j < n; ++j) {
+    tot += w[j];
+  }
+  const double u = f.gu[g];
+  const double uu0 = tot * u / n;
+  const double du = tot / n;
+  double ww = 0;
+  int j = 0;
+  for (int i = 0; i < n; ++i) {
+    const double uu = uu0 + static_cast<double>(i) * du;
+    while (ww < uu && j < n) {
+      ww += w[j];
+      ++j;
+    }
+    idx[i] = j == 0 ? 0 : j - 1;
+  }
+  f.gflag[g] = 0;
+}
+
+}  // namespace engine
+}  // namespace dust2gpu

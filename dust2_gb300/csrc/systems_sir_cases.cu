@@ -1,0 +1,6 @@
+// Registers the sir_cases system with the engine (one system per
+// translation unit so the library compiles in parallel).
+#include "engine/factory.cuh"
+#include "systems/sir_cases.hpp"
+
+DUST2_REGISTER_SYSTEM(dust2gpu::systems::sir_cases);

@@ -1,0 +1,257 @@
+/*
+ * dust2_gb300: C ABI of the GPU engine for dust2's data-parallel hot path
+ * (batched stepping of discrete-time stochastic systems, the bootstrap
+ * particle filter, and the dopri5 integrator of continuous-time systems).
+ *
+ * dust2 reaches its engines through generated `.Call` entry points, one
+ * family per system: `_<pkg>_dust2_system_<name>_<verb>` and
+ * `_<pkg>_dust2_filter_<name>_<verb>` (src/cpp11.cpp:302-405, templates
+ * inst/template/*.cpp), implemented by the adaptors in
+ * inst/include/dust2/r/{system,filter,helpers}.hpp and
+ * r/{discrete,continuous}/{system,filter}.hpp.  Each function below
+ * replaces one of those verbs; the reference function it replaces is
+ * named beside it (paths relative to the dust2 source tree).
+ *
+ * Conventions
+ *   - Plain C types only.  Handles are opaque.
+ *   - Every function returns DUST2_GB300_OK (0) or DUST2_GB300_ERROR (1);
+ *     on error, dust2_gb300_last_error() returns the message (thread
+ *     local), in the wording of the reference's R errors where one exists.
+ *   - Indices are 0-based (the R layer subtracts 1, as
+ *     r/helpers.hpp:279-306 does).
+ *   - Parameters are a flat double array of n_groups rows laid out by the
+ *     system's parameter table (dust2_gb300_system_info); NaN marks a
+ *     value that was not given (the default applies, or, on update, the
+ *     current value is kept).
+ *   - State arrays use dust2's dimension order: state fastest, then
+ *     particle, then group (then time for simulate).
+ *   - Random number generator state is 4 uint64 words (32 bytes) per
+ *     stream, in stream order; raw bytes are the little-endian words, as
+ *     dust2's raw vectors.
+ *   - Calls are synchronous: inputs are read and outputs written before
+ *     the function returns.
+ */
+#ifndef DUST2_GB300_H
+#define DUST2_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DUST2_GB300_OK 0
+#define DUST2_GB300_ERROR 1
+
+typedef struct dust2_gb300_system dust2_gb300_system;
+typedef struct dust2_gb300_filter dust2_gb300_filter;
+
+/* Adaptive-stepper controls (R/interface-continuous.R dust_ode_control,
+ * inst/include/dust2/continuous/control.hpp:11-27). */
+typedef struct dust2_gb300_ode_control {
+  int32_t max_steps;
+  double atol;
+  double rtol;
+  double step_size_min;
+  double step_size_max;
+  const double* critical_times;
+  size_t n_critical_times;
+  int32_t debug_record_step_times;
+} dust2_gb300_ode_control;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* ABI version of this header. */
+int dust2_gb300_abi_version(void);
+
+/* Copy the calling thread's last error message into buf (NUL-terminated,
+ * truncated to len); returns the full message length. */
+size_t dust2_gb300_last_error(char* buf, size_t len);
+
+/* Number of CUDA devices visible (0 without a GPU). */
+int dust2_gb300_device_count(int32_t* n);
+
+/* Names of the compiled-in systems, comma separated. */
+int dust2_gb300_systems(char* buf, size_t len);
+
+/* JSON description of a system: time type, parameter table (name, length,
+ * default, required, constant), data columns.  Replaces the generator
+ * metadata R reads from `[[dust2::...]]` annotations (R/metadata.R). */
+int dust2_gb300_system_info(const char* name, char* json, size_t len);
+
+/* The first n_streams generator streams of a seed (same seed forms as
+ * dust2_gb300_system_alloc), 4 words per stream.  Replaces the monty
+ * calls of R/interface-filter.R:120-124 (filter_rng_state:
+ * monty_rng_create + monty_rng_state). */
+int dust2_gb300_rng_streams(const uint64_t* seed, size_t seed_len,
+                            size_t n_streams, uint64_t* out);
+
+/* ---- systems (r/system.hpp, r/discrete/system.hpp,
+ *      r/continuous/system.hpp) ------------------------------------------ */
+
+/* dust2_discrete_alloc / dust2_continuous_alloc
+ * (r/discrete/system.hpp:13-55, r/continuous/system.hpp:13-50).
+ * seed: either 1 word (an integer seed, expanded with SplitMix64) or
+ * 4 * k words (raw state of the first k streams; further streams are
+ * successive jumps).  dt is ignored for continuous-time systems, control
+ * for discrete-time ones (may be NULL: defaults). */
+int dust2_gb300_system_alloc(const char* name, const double* pars,
+                             size_t n_groups, size_t n_particles,
+                             double time, double dt,
+                             const dust2_gb300_ode_control* control,
+                             const uint64_t* seed, size_t seed_len,
+                             int32_t deterministic,
+                             dust2_gb300_system** out);
+
+/* Finalizer of the external pointer (r/discrete/system.hpp:46). */
+int dust2_gb300_system_free(dust2_gb300_system* sys);
+
+/* Dimensions: n_state, n_particles (per group), n_groups. */
+int dust2_gb300_system_dim(const dust2_gb300_system* sys, size_t* n_state,
+                           size_t* n_particles, size_t* n_groups);
+
+/* dust2_system_state (r/system.hpp:89-161), full state:
+ * out has n_state * n_particles * n_groups doubles. */
+int dust2_gb300_system_state(dust2_gb300_system* sys, double* out);
+
+/* dust2_system_set_state (r/system.hpp:189-195 via
+ * internals.hpp:10-62): value holds len(index_state or n_state) *
+ * len(index_particle or n_particles, or 1 when recycling particles) *
+ * len(index_group or n_groups, or 1 when recycling groups) doubles; any
+ * index may be NULL (all). */
+int dust2_gb300_system_set_state(dust2_gb300_system* sys, const double* value,
+                                 const size_t* index_state, size_t n_index_state,
+                                 const size_t* index_particle,
+                                 size_t n_index_particle,
+                                 const size_t* index_group, size_t n_index_group,
+                                 int32_t recycle_particle,
+                                 int32_t recycle_group);
+
+/* dust2_system_set_state_initial (r/system.hpp:182-187). */
+int dust2_gb300_system_set_state_initial(dust2_gb300_system* sys);
+
+/* dust2_system_time / dust2_system_set_time (r/system.hpp:163-168,
+ * 240-247). */
+int dust2_gb300_system_time(dust2_gb300_system* sys, double* time);
+int dust2_gb300_system_set_time(dust2_gb300_system* sys, double time);
+
+/* dust2_system_rng_state / dust2_system_set_rng_state
+ * (r/system.hpp:223-238): 4 * n_particles * n_groups words. */
+int dust2_gb300_system_rng_state(dust2_gb300_system* sys, uint64_t* out);
+int dust2_gb300_system_set_rng_state(dust2_gb300_system* sys,
+                                     const uint64_t* state, size_t len);
+
+/* dust2_system_update_pars (r/system.hpp:249-254, r/helpers.hpp
+ * update_pars): pars has one row per group (or per entry of index_group
+ * when given). */
+int dust2_gb300_system_update_pars(dust2_gb300_system* sys,
+                                   const double* pars,
+                                   const size_t* index_group,
+                                   size_t n_index_group);
+
+/* dust2_system_run_to_time (r/system.hpp:75-87). */
+int dust2_gb300_system_run_to_time(dust2_gb300_system* sys, double time);
+
+/* dust2_system_simulate (r/system.hpp:286-327): out has
+ * len(index_state or n_state) * n_particles * n_groups * n_times doubles. */
+int dust2_gb300_system_simulate(dust2_gb300_system* sys, const double* times,
+                                size_t n_times, const size_t* index_state,
+                                size_t n_index_state, double* out);
+
+/* dust2_system_reorder (r/system.hpp:199-221): index has
+ * n_particles * n_groups entries, each a particle index within its group. */
+int dust2_gb300_system_reorder(dust2_gb300_system* sys, const size_t* index,
+                               size_t len);
+
+/* dust2_system_compare_data (r/system.hpp:258-284): data holds
+ * n_groups_data (1 or n_groups) rows of the system's data columns (NaN =
+ * missing); out has n_particles * n_groups doubles. */
+int dust2_gb300_system_compare_data(dust2_gb300_system* sys,
+                                    const double* data, size_t n_groups_data,
+                                    double* out);
+
+/* dust2_system_internals (r/continuous/system.hpp:60-159), per particle:
+ * step_size, error, n_steps, n_steps_accepted, n_steps_rejected.
+ * Discrete-time systems have none (returns an error). */
+int dust2_gb300_system_internals(dust2_gb300_system* sys, double* step_size,
+                                 double* error, int64_t* n_steps,
+                                 int64_t* n_steps_accepted,
+                                 int64_t* n_steps_rejected);
+
+/* Recorded step times of one particle (control.debug_record_step_times);
+ * writes at most cap values and the total count to *n. */
+int dust2_gb300_system_step_times(dust2_gb300_system* sys, size_t particle,
+                                  double* out, size_t cap, size_t* n);
+
+/* ---- filters (r/filter.hpp, r/discrete/filter.hpp) -------------------- */
+
+/* dust2_discrete_filter_alloc (r/discrete/filter.hpp:13-88).
+ * time: n_time data times; data: n_time * n_groups_data rows of the
+ * system's data columns, time-major (r/helpers.hpp:404-427).  seed as for
+ * systems; the n_groups * (n_particles + 2) streams are split per group
+ * into 2 filter streams and n_particles particle streams. */
+int dust2_gb300_filter_alloc(const char* name, const double* pars,
+                             size_t n_groups, size_t n_particles,
+                             double time_start, const double* time,
+                             size_t n_time, const double* data,
+                             size_t n_groups_data, double dt,
+                             const uint64_t* seed, size_t seed_len,
+                             dust2_gb300_filter** out);
+
+/* As dust2_gb300_filter_alloc with a particle count per group (groups of
+ * uneven size share one launch; dust2 itself requires equal counts). */
+int dust2_gb300_filter_alloc_uneven(const char* name, const double* pars,
+                                    size_t n_groups,
+                                    const size_t* n_particles,
+                                    double time_start, const double* time,
+                                    size_t n_time, const double* data,
+                                    size_t n_groups_data, double dt,
+                                    const uint64_t* seed, size_t seed_len,
+                                    dust2_gb300_filter** out);
+
+int dust2_gb300_filter_free(dust2_gb300_filter* filter);
+
+/* n_state, total particles, n_groups and number of data times. */
+int dust2_gb300_filter_dim(const dust2_gb300_filter* filter, size_t* n_state,
+                           size_t* n_particles_total, size_t* n_groups,
+                           size_t* n_time);
+
+/* dust2_filter_run (r/filter.hpp:112-143): initial may be NULL (system
+ * initial conditions) or a full state; index_group may be NULL (all
+ * groups).  ll receives one log-likelihood per group run. */
+int dust2_gb300_filter_run(dust2_gb300_filter* filter, const double* initial,
+                           const size_t* index_group, size_t n_index_group,
+                           double* ll);
+
+/* dust2_filter_update_pars (r/filter.hpp:101-110). */
+int dust2_gb300_filter_update_pars(dust2_gb300_filter* filter,
+                                   const double* pars,
+                                   const size_t* index_group,
+                                   size_t n_index_group);
+
+/* dust2_filter_rng_state / dust2_filter_set_rng_state
+ * (r/filter.hpp:273-329): per group, 2 filter streams then the group's
+ * particle streams, 4 words each. */
+int dust2_gb300_filter_rng_state(dust2_gb300_filter* filter, uint64_t* out,
+                                 size_t len);
+int dust2_gb300_filter_set_rng_state(dust2_gb300_filter* filter,
+                                     const uint64_t* state, size_t len);
+
+/* dust2_filter_last_state (r/filter.hpp:233-271): full final state, or
+ * with select_random_particle one particle per group chosen from the
+ * group's second filter stream (filter.hpp:130-138). */
+int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
+                                  int32_t select_random_particle,
+                                  double* out);
+
+/* Groups whose resampling was recomputed serially so far (diagnostic of
+ * the exact-resampling check). */
+int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,
+                                        int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,66 @@
+"""TEST INFRASTRUCTURE (oracle): compile the CPU oracle.
+
+* oracle/port/oracle.cpp -> oracle/_build/liboracle.so, everywhere (g++,
+  OpenMP, no floating-point contraction).
+* oracle/ref_driver.cpp -> oracle/_ref/libdust2_ref.so, only where the
+  reference sources exist (oracle/Makefile reads them in place).
+
+Only tests, the smoke check and the CPU-baseline leg of bench.py load
+these libraries.
+"""
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent
+CSRC = REPO / "dust2_gb300" / "csrc"
+PORT_SRC = HERE / "port" / "oracle.cpp"
+PORT_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libdust2_ref.so"
+REF_INCLUDE = Path(os.environ.get("DUST2_REF",
+                                  "/root/reference/inst/include"))
+
+
+def _inputs():
+    return ([PORT_SRC] + list((CSRC / "dust2gpu").glob("*.hpp")) +
+            list((CSRC / "systems").glob("*.hpp")) +
+            [CSRC / "engine" / "error_text.hpp", Path(__file__)])
+
+
+def build_port(force=False):
+    newest = max(p.stat().st_mtime for p in _inputs())
+    if not force and PORT_LIB.exists() and PORT_LIB.stat().st_mtime >= newest:
+        return PORT_LIB
+    PORT_LIB.parent.mkdir(exist_ok=True)
+    tmp = PORT_LIB.with_suffix(".so.tmp")
+    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared",
+           "-ffp-contract=off", "-fno-strict-aliasing", "-I", str(CSRC),
+           str(PORT_SRC), "-o", str(tmp)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, PORT_LIB)
+    return PORT_LIB
+
+
+def build_ref(force=False):
+    """Build the reference-engine oracle; None when sources are absent."""
+    if not (REF_INCLUDE / "dust2" / "filter.hpp").exists():
+        return None
+    cmd = ["make", "-s", "-C", str(HERE), f"REF={REF_INCLUDE}"]
+    if force:
+        subprocess.run(["make", "-s", "-C", str(HERE), "clean"], check=True)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"reference build failed:\n{res.stdout}\n"
+                           f"{res.stderr}")
+    return REF_LIB
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    print(build_port(force))
+    print(build_ref(force))

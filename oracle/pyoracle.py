@@ -1,0 +1,201 @@
+"""TEST INFRASTRUCTURE (oracle): ctypes access to the CPU oracle.
+
+`port` is the CPU restatement (oracle/port/oracle.cpp, built everywhere);
+`ref` is dust2's own engine compiled from the reference sources with the
+project's monty stand-in (oracle/ref_driver.cpp, built only where the
+reference tree exists).  Both expose the same functions, so tests can
+run one against the other and against the CUDA engine.
+"""
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libdust2_ref.so"
+
+_d = ctypes.POINTER(ctypes.c_double)
+_u = ctypes.POINTER(ctypes.c_uint64)
+_i = ctypes.POINTER(ctypes.c_int)
+_l = ctypes.POINTER(ctypes.c_int64)
+_c = ctypes.c_char_p
+_n = ctypes.c_int
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _dp(a):
+    return None if a is None else np.ascontiguousarray(
+        a, dtype=np.float64).ctypes.data_as(_d)
+
+
+class Oracle:
+    """One oracle library (port or reference build)."""
+
+    def __init__(self, path, kind):
+        self.kind = kind
+        self.path = Path(path)
+        self.lib = ctypes.CDLL(str(path))
+        p = "oracle_" if kind == "port" else "ref_"
+        self.prefix = p
+        lib = self.lib
+        self._sim = getattr(lib, p + "discrete_simulate")
+        self._cmp = getattr(lib, p + "compare")
+        self._flt = getattr(lib, p + "filter_run")
+        self._ode = getattr(lib, p + "ode_simulate")
+        self._slw = getattr(lib, p + "scale_log_weights")
+        self._slw.restype = ctypes.c_double
+        self._slw.argtypes = [_n, _d]
+        self._rsw = getattr(lib, p + "resample_weight")
+        self._rsw.restype = None
+        self._rsw.argtypes = [_n, _d, ctypes.c_double, _l]
+        if kind == "port":
+            lib.oracle_max_threads.restype = ctypes.c_int
+
+    def max_threads(self):
+        return self.lib.oracle_max_threads() if self.kind == "port" else 1
+
+    def _call(self, fn, *args):
+        err = ctypes.create_string_buffer(4096)
+        rc = fn(*args, err, len(err))
+        if rc != 0:
+            raise OracleError(err.value.decode())
+
+    def discrete_simulate(self, name, pars, n_groups, n_particles, time, dt,
+                          rng, times, deterministic=False, initial=None,
+                          n_threads=1):
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        rng = np.ascontiguousarray(rng, dtype=np.uint64)
+        n_total = n_groups * n_particles
+        n_state = None
+        out = None
+        # the state size is not known here; ask with a generous buffer
+        buf = np.empty(times.size * n_total * 128)
+        rng_out = np.empty(4 * n_total, dtype=np.uint64)
+        args = [_c(name.encode()), _dp(pars), _n(n_groups), _n(n_particles),
+                ctypes.c_double(time), ctypes.c_double(dt),
+                rng.ctypes.data_as(_u), _n(int(deterministic)),
+                _dp(initial), _dp(times), _n(times.size), _dp(buf),
+                rng_out.ctypes.data_as(_u)]
+        if self.kind == "port":
+            args.append(_n(n_threads))
+        self._call(self._sim, *args)
+        n_state = None
+        return buf, rng_out
+
+    def filter_run(self, name, pars, n_particles, time_start, times, data,
+                   n_groups_data, dt, rng, n_runs=1, initial=None,
+                   index_group=None, n_state=None, n_threads=1):
+        """n_particles: list per group (port) or equal counts (ref)."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        rng = np.ascontiguousarray(rng, dtype=np.uint64)
+        npg = list(n_particles)
+        G = len(npg)
+        n_total = sum(npg)
+        ll = np.full(n_runs * G, np.nan)
+        state = np.empty(n_total * (n_state or 128))
+        rng_out = np.empty(4 * (n_total + 2 * G), dtype=np.uint64)
+        if self.kind == "port":
+            npa = np.ascontiguousarray(npg, dtype=np.intc)
+            ig = None if index_group is None else np.ascontiguousarray(
+                index_group, dtype=np.intc)
+            self._call(self._flt, _c(name.encode()), _dp(pars), _n(G),
+                       npa.ctypes.data_as(_i), ctypes.c_double(time_start),
+                       _dp(times), _n(times.size), _dp(data),
+                       _n(n_groups_data), ctypes.c_double(dt),
+                       rng.ctypes.data_as(_u), _n(n_runs), _dp(initial),
+                       None if ig is None else ig.ctypes.data_as(_i),
+                       _n(0 if ig is None else ig.size), _dp(ll), _dp(state),
+                       rng_out.ctypes.data_as(_u), _n(n_threads))
+        else:
+            if len(set(npg)) != 1 or index_group is not None:
+                raise OracleError("the reference filter needs equal counts")
+            self._call(self._flt, _c(name.encode()), _dp(pars), _n(G),
+                       _n(npg[0]), ctypes.c_double(time_start), _dp(times),
+                       _n(times.size), _dp(data), _n(n_groups_data),
+                       ctypes.c_double(dt), rng.ctypes.data_as(_u),
+                       _n(n_runs), _dp(initial), _dp(ll), _dp(state),
+                       rng_out.ctypes.data_as(_u))
+        return ll.reshape(n_runs, G), state, rng_out
+
+    def compare(self, name, pars, n_groups, n_particles, time, state, data,
+                n_groups_data, rng):
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        rng = np.ascontiguousarray(rng, dtype=np.uint64)
+        n_total = n_groups * n_particles
+        out = np.empty(n_total)
+        rng_out = np.empty(4 * n_total, dtype=np.uint64)
+        self._call(self._cmp, _c(name.encode()), _dp(pars), _n(n_groups),
+                   _n(n_particles), ctypes.c_double(time), _dp(state),
+                   _dp(data), _n(n_groups_data), rng.ctypes.data_as(_u),
+                   _dp(out), rng_out.ctypes.data_as(_u))
+        return out, rng_out
+
+    def ode_simulate(self, name, pars, n_groups, n_particles, time, times,
+                     n_state, max_steps=10000, atol=1e-6, rtol=1e-6,
+                     step_size_min=np.finfo(float).eps,
+                     step_size_max=np.inf, critical_times=(), n_threads=1):
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        crit = np.ascontiguousarray(critical_times, dtype=np.float64)
+        n_total = n_groups * n_particles
+        out = np.empty(times.size * n_total * n_state)
+        stats = np.empty(3 * n_total, dtype=np.int64)
+        args = [_c(name.encode()), _dp(pars), _n(n_groups), _n(n_particles),
+                ctypes.c_double(time), _n(max_steps), ctypes.c_double(atol),
+                ctypes.c_double(rtol), ctypes.c_double(step_size_min),
+                ctypes.c_double(step_size_max),
+                crit.ctypes.data_as(_d) if crit.size else None,
+                _n(crit.size), _dp(times), _n(times.size), _dp(out),
+                stats.ctypes.data_as(_l)]
+        if self.kind == "port":
+            args.append(_n(n_threads))
+        self._call(self._ode, *args)
+        return out, stats.reshape(n_total, 3)
+
+    def scale_log_weights(self, w):
+        w = np.array(w, dtype=np.float64)
+        ret = self._slw(w.size, w.ctypes.data_as(_d))
+        return ret, w
+
+    def resample_weight(self, w, u):
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        idx = np.empty(w.size, dtype=np.int64)
+        self._rsw(w.size, w.ctypes.data_as(_d), float(u),
+                  idx.ctypes.data_as(_l))
+        return idx
+
+
+_port = None
+_ref = None
+
+
+def port():
+    """The CPU restatement (builds it if needed)."""
+    global _port
+    if _port is None:
+        from . import build
+        build.build_port()
+        _port = Oracle(PORT_LIB, "port")
+    return _port
+
+
+def ref():
+    """dust2's own engine, or None where the reference build is absent."""
+    global _ref
+    if _ref is None:
+        if not REF_LIB.exists():
+            from . import build
+            if build.build_ref() is None:
+                return None
+        _ref = Oracle(REF_LIB, "ref")
+    return _ref

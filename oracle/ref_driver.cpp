@@ -1,0 +1,438 @@
+// TEST INFRASTRUCTURE (oracle).  Drives dust2's own C++ engine --
+// dust2::dust_discrete, dust2::filter, dust2::dust_continuous and the
+// filter_details helpers, compiled unmodified from the reference tree
+// (inst/include/dust2/...) -- on the project's system classes, and
+// exposes it through a small C interface for the tests and for fixture
+// generation.  Built by oracle/Makefile into oracle/_ref/ only where the
+// reference sources are present; never part of the product.
+//
+// The project's systems (dust2_gb300/csrc/systems/*.hpp) are written to
+// the GPU plugin contract; the adapters below present them to the
+// reference engine in its own plugin contract (vignettes/writing.Rmd;
+// detection in inst/include/dust2/properties.hpp): `packing_state`
+// returns a dust2::packing, `zero_every` a dust2::zero_every_type, and a
+// sampler error recorded in the generator becomes the exception the
+// reference engine expects to catch (discrete/system.hpp:82-84).
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <dust2/continuous/system.hpp>
+#include <dust2/discrete/system.hpp>
+#include <dust2/filter.hpp>
+#include <dust2/filter_details.hpp>
+
+#include "engine/error_text.hpp"
+#include "systems/logistic.hpp"
+#include "systems/seir_age.hpp"
+#include "systems/sir.hpp"
+#include "systems/sir_cases.hpp"
+#include "systems/sirode.hpp"
+#include "systems/walk.hpp"
+
+namespace {
+
+using rng_state_type = dust2gpu::random::rng_state;
+
+void raise_if_error(rng_state_type& rng) {
+  if (rng.err != 0) {
+    dust2gpu::particle_error e{rng.err, rng.err_v0, rng.err_v1};
+    rng.err = 0;
+    throw std::runtime_error(dust2gpu::error_text(e));
+  }
+}
+
+template <typename S>
+dust2::zero_every_type<double> zero_every_of(
+    const typename S::shared_state& shared) {
+  const auto z = S::zero_every(shared);
+  dust2::zero_every_type<double> ret;
+  for (int i = 0; i < z.n; ++i) {
+    std::vector<size_t> idx;
+    for (int s = 0; s < 64 * dust2gpu::ZERO_EVERY_WORDS; ++s) {
+      if (z.has(i, s)) {
+        idx.push_back(s);
+      }
+    }
+    ret.push_back({z.period[i], idx});
+  }
+  return ret;
+}
+
+template <typename S>
+struct ref_discrete {
+  using real_type = double;
+  using rng_state_type = ::rng_state_type;
+  using shared_state = typename S::shared_state;
+  using internal_state = typename S::internal_state;
+  using data_type = typename S::data_type;
+
+  static dust2::packing packing_state(const shared_state& shared) {
+    return dust2::packing{
+      {"state", {static_cast<size_t>(S::n_state(shared))}}};
+  }
+  static void initial(real_type time, const shared_state& shared,
+                      internal_state& internal, rng_state_type& rng,
+                      real_type* state_next) {
+    S::initial(time, shared, internal, rng, state_next);
+    raise_if_error(rng);
+  }
+  static void update(real_type time, real_type dt, const real_type* state,
+                     const shared_state& shared, internal_state& internal,
+                     rng_state_type& rng, real_type* state_next) {
+    S::update(time, dt, state, shared, internal, rng, state_next);
+    raise_if_error(rng);
+  }
+  static real_type compare_data(const real_type time, const real_type* state,
+                                const data_type& data,
+                                const shared_state& shared,
+                                internal_state& internal,
+                                rng_state_type& rng) {
+    const auto ret = S::compare_data(time, state, data, shared, internal, rng);
+    raise_if_error(rng);
+    return ret;
+  }
+  static dust2::zero_every_type<real_type> zero_every(
+      const shared_state& shared) {
+    return zero_every_of<S>(shared);
+  }
+};
+
+template <typename S>
+struct ref_continuous {
+  using real_type = double;
+  using rng_state_type = ::rng_state_type;
+  using shared_state = typename S::shared_state;
+  using internal_state = typename S::internal_state;
+  using data_type = typename S::data_type;
+
+  static dust2::packing packing_state(const shared_state& shared) {
+    return dust2::packing{
+      {"state", {static_cast<size_t>(S::n_state(shared))}}};
+  }
+  static void initial(real_type time, const shared_state& shared,
+                      internal_state& internal, rng_state_type& rng,
+                      real_type* state_next) {
+    S::initial(time, shared, internal, rng, state_next);
+  }
+  static void rhs(real_type time, const real_type* state,
+                  const shared_state& shared, internal_state& internal,
+                  real_type* deriv) {
+    S::rhs(time, state, shared, internal, deriv);
+  }
+  static real_type compare_data(const real_type time, const real_type* state,
+                                const data_type& data,
+                                const shared_state& shared,
+                                internal_state& internal,
+                                rng_state_type& rng) {
+    return S::compare_data(time, state, data, shared, internal, rng);
+  }
+  static dust2::zero_every_type<real_type> zero_every(
+      const shared_state& shared) {
+    return zero_every_of<S>(shared);
+  }
+};
+
+// logistic: an ODE with one output variable (size_output / output).
+struct ref_logistic {
+  using S = dust2gpu::systems::logistic;
+  using real_type = double;
+  using rng_state_type = ::rng_state_type;
+  using shared_state = S::shared_state;
+  using internal_state = S::internal_state;
+  using data_type = S::data_type;
+
+  static dust2::packing packing_state(const shared_state& shared) {
+    return dust2::packing{{"x", {static_cast<size_t>(shared.n)}},
+                          {"total", {}}};
+  }
+  static size_t size_output() {
+    return 1;
+  }
+  static void initial(real_type time, const shared_state& shared,
+                      internal_state& internal, rng_state_type& rng,
+                      real_type* state_next) {
+    S::initial(time, shared, internal, rng, state_next);
+  }
+  static void rhs(real_type time, const real_type* state,
+                  const shared_state& shared, internal_state& internal,
+                  real_type* deriv) {
+    S::rhs(time, state, shared, internal, deriv);
+  }
+  static void output(real_type time, real_type* state,
+                     const shared_state& shared, internal_state& internal) {
+    S::output(time, state, shared, internal);
+  }
+};
+
+template <typename T>
+struct tag {
+  using type = T;
+};
+
+template <typename F>
+bool dispatch_discrete(const std::string& name, F f) {
+  using namespace dust2gpu::systems;
+  if (name == "sir") {
+    f(tag<ref_discrete<sir>>{}, tag<sir>{});
+  } else if (name == "sir_cases") {
+    f(tag<ref_discrete<sir_cases>>{}, tag<sir_cases>{});
+  } else if (name == "walk") {
+    f(tag<ref_discrete<walk>>{}, tag<walk>{});
+  } else if (name == "seir_age") {
+    f(tag<ref_discrete<seir_age>>{}, tag<seir_age>{});
+  } else {
+    return false;
+  }
+  return true;
+}
+
+template <typename S>
+std::vector<typename S::shared_state> shared_of(const double* pars,
+                                                int n_groups) {
+  const int np = dust2gpu::parameter_length<S>();
+  std::vector<typename S::shared_state> ret;
+  for (int g = 0; g < n_groups; ++g) {
+    ret.push_back(S::build_shared(pars + static_cast<size_t>(g) * np));
+  }
+  return ret;
+}
+
+void set_err(char* err, int err_len, const std::string& msg) {
+  if (err != nullptr && err_len > 0) {
+    std::strncpy(err, msg.c_str(), err_len - 1);
+    err[err_len - 1] = '\0';
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+// dust_discrete: set initial state (or `initial`), then run_to_time for
+// each of `times`, recording the full state after each.  out:
+// [n_times][group][particle][state]; rng_out: final generator state.
+int ref_discrete_simulate(const char* name, const double* pars, int n_groups,
+                          int n_particles, double time, double dt,
+                          const uint64_t* rng, int deterministic,
+                          const double* initial, const double* times,
+                          int n_times, double* out, uint64_t* rng_out,
+                          char* err, int err_len) {
+  try {
+    bool ok = dispatch_discrete(name, [&](auto t, auto s) {
+      using T = typename decltype(t)::type;
+      using S = typename decltype(s)::type;
+      auto shared = shared_of<S>(pars, n_groups);
+      std::vector<typename T::internal_state> internal(n_groups);
+      const size_t n_total = static_cast<size_t>(n_particles) * n_groups;
+      std::vector<uint64_t> seed(rng, rng + 4 * n_total);
+      dust2::dust_discrete<T> sys(shared, internal, time, dt, n_particles,
+                                  seed, deterministic != 0, 1);
+      if (initial == nullptr) {
+        sys.set_state_initial(sys.all_groups());
+      } else {
+        sys.set_state(initial, {}, {}, {}, false, false);
+      }
+      const size_t len = sys.state().size();
+      for (int i = 0; i < n_times; ++i) {
+        sys.run_to_time(times[i], sys.all_groups());
+        std::copy(sys.state().begin(), sys.state().end(), out + i * len);
+      }
+      const auto r = sys.rng_state();
+      std::copy(r.begin(), r.end(), rng_out);
+    });
+    if (!ok) {
+      throw std::runtime_error(std::string("unknown system ") + name);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// dust_discrete::compare_data on a given state.
+int ref_compare(const char* name, const double* pars, int n_groups,
+                int n_particles, double time, const double* state,
+                const double* data, int n_groups_data, const uint64_t* rng,
+                double* out, uint64_t* rng_out, char* err, int err_len) {
+  try {
+    bool ok = dispatch_discrete(name, [&](auto t, auto s) {
+      using T = typename decltype(t)::type;
+      using S = typename decltype(s)::type;
+      if constexpr (dust2gpu::has_compare_data<S>::value) {
+        auto shared = shared_of<S>(pars, n_groups);
+        std::vector<typename T::internal_state> internal(n_groups);
+        const size_t n_total = static_cast<size_t>(n_particles) * n_groups;
+        std::vector<uint64_t> seed(rng, rng + 4 * n_total);
+        dust2::dust_discrete<T> sys(shared, internal, time, 1.0, n_particles,
+                                    seed, false, 1);
+        sys.set_state(state, {}, {}, {}, false, false);
+        std::vector<typename S::data_type> d;
+        const int nd = sizeof(typename S::data_type) / sizeof(double);
+        for (int g = 0; g < n_groups_data; ++g) {
+          d.push_back(S::build_data(data + g * nd));
+        }
+        std::vector<double> o(n_total);
+        sys.compare_data(d.begin(), n_groups_data, sys.all_groups(),
+                         o.begin());
+        std::copy(o.begin(), o.end(), out);
+        const auto r = sys.rng_state();
+        std::copy(r.begin(), r.end(), rng_out);
+      } else {
+        throw std::runtime_error("system has no compare_data");
+      }
+    });
+    if (!ok) {
+      throw std::runtime_error(std::string("unknown system ") + name);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// dust2::filter over dust_discrete, following dust2_discrete_filter_alloc
+// (r/discrete/filter.hpp:13-88) for the stream split.  Runs the filter
+// n_runs times (the object persists between runs, as
+// dust_likelihood_run does); ll_out: [n_runs][n_groups].  initial (may be
+// null) is applied before every run in place of the initial conditions.
+int ref_filter_run(const char* name, const double* pars, int n_groups,
+                   int n_particles, double time_start, const double* times,
+                   int n_times, const double* data, int n_groups_data,
+                   double dt, const uint64_t* rng, int n_runs,
+                   const double* initial, double* ll_out, double* state_out,
+                   uint64_t* rng_out, char* err, int err_len) {
+  try {
+    bool ok = dispatch_discrete(name, [&](auto t, auto s) {
+      using T = typename decltype(t)::type;
+      using S = typename decltype(s)::type;
+      if constexpr (dust2gpu::has_compare_data<S>::value) {
+        auto shared = shared_of<S>(pars, n_groups);
+        std::vector<typename T::internal_state> internal(n_groups);
+        std::vector<uint64_t> seed_filter, seed_system;
+        for (int g = 0; g < n_groups; ++g) {
+          const uint64_t* it = rng + static_cast<size_t>(g) * 4 *
+            (n_particles + 2);
+          seed_filter.insert(seed_filter.end(), it, it + 8);
+          seed_system.insert(seed_system.end(), it + 8,
+                             it + 4 * (n_particles + 2));
+        }
+        dust2::dust_discrete<T> sys(shared, internal, time_start, dt,
+                                    n_particles, seed_system, false, 1);
+        std::vector<double> tt(times, times + n_times);
+        std::vector<typename S::data_type> d;
+        const int nd = sizeof(typename S::data_type) / sizeof(double);
+        for (int i = 0; i < n_times * n_groups_data; ++i) {
+          d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+        }
+        dust2::filter<dust2::dust_discrete<T>> obj(sys, time_start, tt, d,
+                                                   seed_filter);
+        for (int r = 0; r < n_runs; ++r) {
+          if (initial != nullptr) {
+            obj.sys.set_state(initial, {}, {}, {}, false, false);
+          }
+          obj.run(initial == nullptr, false, {}, {}, obj.sys.all_groups());
+          const auto& ll = obj.last_log_likelihood();
+          std::copy(ll.begin(), ll.end(), ll_out + r * n_groups);
+        }
+        std::copy(obj.sys.state().begin(), obj.sys.state().end(), state_out);
+        // the raw layout of r/filter.hpp:273-298
+        const auto sf = obj.rng_state();
+        const auto ss = obj.sys.rng_state();
+        size_t pos = 0;
+        for (int g = 0; g < n_groups; ++g) {
+          for (int w = 0; w < 8; ++w) {
+            rng_out[pos++] = sf[g * 8 + w];
+          }
+          for (int w = 0; w < 4 * n_particles; ++w) {
+            rng_out[pos++] = ss[static_cast<size_t>(g) * 4 * n_particles + w];
+          }
+        }
+      } else {
+        throw std::runtime_error("system has no compare_data");
+      }
+    });
+    if (!ok) {
+      throw std::runtime_error(std::string("unknown system ") + name);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// dust_continuous: initial conditions, then run_to_time through `times`,
+// recording state; stats_out: [particle][3] n_steps, accepted, rejected.
+int ref_ode_simulate(const char* name, const double* pars, int n_groups,
+                     int n_particles, double time, int max_steps,
+                     double atol, double rtol, double step_size_min,
+                     double step_size_max, const double* critical,
+                     int n_critical, const double* times, int n_times,
+                     double* out, int64_t* stats_out, char* err,
+                     int err_len) {
+  try {
+    auto body = [&](auto t, auto s) {
+      using T = typename decltype(t)::type;
+      using S = typename decltype(s)::type;
+      auto shared = shared_of<S>(pars, n_groups);
+      std::vector<typename T::internal_state> internal(n_groups);
+      std::vector<double> crit(critical, critical + n_critical);
+      dust2::ode::control<double> ctl(max_steps, atol, rtol, step_size_min,
+                                      step_size_max, crit, false, false);
+      std::vector<uint64_t> seed{42};
+      dust2::dust_continuous<T> sys(shared, internal, time, 0, ctl,
+                                    n_particles, seed, true, 1);
+      sys.set_state_initial(sys.all_groups());
+      const size_t len = sys.state().size();
+      for (int i = 0; i < n_times; ++i) {
+        sys.run_to_time(times[i], sys.all_groups());
+        const auto& st = sys.state();
+        std::copy(st.begin(), st.end(), out + i * len);
+      }
+      const auto& oi = sys.ode_internals();
+      for (size_t k = 0; k < oi.size(); ++k) {
+        stats_out[3 * k] = oi[k].n_steps;
+        stats_out[3 * k + 1] = oi[k].n_steps_accepted;
+        stats_out[3 * k + 2] = oi[k].n_steps_rejected;
+      }
+    };
+    const std::string nm(name);
+    if (nm == "sirode") {
+      using S = dust2gpu::systems::sirode;
+      body(tag<ref_continuous<S>>{}, tag<S>{});
+    } else if (nm == "logistic") {
+      body(tag<ref_logistic>{}, tag<dust2gpu::systems::logistic>{});
+    } else {
+      throw std::runtime_error("unknown system " + nm);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// inst/include/dust2/filter_details.hpp:11-39 (w updated in place)
+double ref_scale_log_weights(int n, double* w) {
+  std::vector<double> v(w, w + n);
+  const double ret = dust2::details::scale_log_weights<double>(n, v.begin());
+  std::copy(v.begin(), v.end(), w);
+  return ret;
+}
+
+// inst/include/dust2/filter_details.hpp:45-74
+void ref_resample_weight(int n, const double* w, double u, int64_t* idx) {
+  std::vector<double> v(w, w + n);
+  std::vector<size_t> i(n);
+  dust2::details::resample_weight<double>(n, v.cbegin(), u, i.begin());
+  for (int k = 0; k < n; ++k) {
+    idx[k] = static_cast<int64_t>(i[k]);
+  }
+}
+
+}  // extern "C"
