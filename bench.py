@@ -1,0 +1,456 @@
+"""Benchmark: batched SIR particle filter, particle-steps/s on one GB300.
+
+Workload (default, `--workload sir_batched`): 64 parameter groups of the
+stochastic SIR model (beta ~ U(0.1, 0.5), gamma ~ U(0.05, 0.2), N = 1e6,
+I0 ~ U{1..100}), uneven particle counts round(2^U(9, 15)) per group from
+seed 1, 200 daily observations per group simulated from the model plus
+Poisson noise, dt = 0.25 (4 steps per observation), one likelihood
+evaluation of all groups per step.  Data are synthetic (the model itself
+generates them; there is no external dataset).
+
+Reported numbers (one JSON line on rank 0):
+  value   particle-steps/s of whole likelihood runs, device-timed with CUDA
+          events on the filter's stream, inputs resident on the device, L2
+          flushed (256 MB write) between timed runs;
+  e2e     the same metric through the public API (dust_likelihood_run:
+          parameters copied host->device, log-likelihoods device->host,
+          every step), wall-clock;
+  roofline  for the dominant kernel (the step+compare kernel) against the
+          FP64 pipe: executed FP64 operations per particle-step (ncu SASS
+          counters of this kernel, stated in the constant below) times the
+          particle-steps of one launch, over the kernel's device time
+          measured live with CUDA events inside the timed runs; peak from a
+          DFMA microbenchmark run in this process;
+  cpu_baseline  the CPU restatement of dust2's engine (OpenMP over all
+          host cores) on a bounded sample of the same workload.
+
+`--impl reference` times that CPU implementation alone (the reference arm).
+Multi-GPU (torchrun) runs independent replicas, one per GPU: the path has
+no cross-group exchange.
+"""
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+# Executed FP64 operations (DADD + DMUL + 2 DFMA, per thread) per
+# particle-step of the step+compare kernel on this workload, from the ncu
+# SASS counters summarised in profiles/ (see the design doc).  None until
+# measured.
+FP64_OPS_PER_PARTICLE_STEP = None
+STEPS_PER_OBS = 4  # dt = 0.25, daily observations
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--workload", default="sir_batched",
+                   choices=["sir_batched", "sir_small"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=12.0,
+                   help="target CPU time of the bounded CPU sample")
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,"
+                 "noheader,nounits", "-lms", "200", "-i", str(self.gpu_index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops():
+    """DFMA throughput microbenchmark (FP64 FMA chains, all SMs)."""
+    import ctypes
+    from dust2_gb300 import _lib
+    t = ctypes.c_double()
+    _lib.check(_lib.lib().dust2_gb300_fp64_peak(ctypes.byref(t)))
+    return t.value
+
+
+def build_workload(name, simulate):
+    from dust2_gb300 import workloads
+    if name == "sir_batched":
+        return workloads.sir_batched(simulate)
+    w = workloads.sir_small(simulate)
+    w["data"] = w["data"].reshape(-1, 1)
+    w["n_particles"] = [w["n_particles"]]
+    return w
+
+
+def data_columns(w):
+    times = w["times"]
+    G = len(w["n_particles"])
+    cols = {"time": np.repeat(times, G), "incidence": w["data"].ravel()}
+    if G > 1:
+        cols["group"] = np.tile(np.arange(1, G + 1), times.size)
+    return cols
+
+
+def run_cpu(w, n_groups, n_threads, n_runs=1):
+    """Run the CPU oracle on the first n_groups groups of the workload;
+    returns (seconds per run, particle-steps per run)."""
+    from oracle import pyoracle
+    import dust2_gb300 as d
+    port = pyoracle.port()
+    npg = w["n_particles"][:n_groups]
+    G_all = len(w["n_particles"])
+    gen = d.sir_cases()
+    npar = gen.n_pars
+    pars = np.asarray(w["pars"]).reshape(G_all, npar)[:n_groups].ravel()
+    data = np.asarray(w["data"]).reshape(w["times"].size, G_all)[:, :n_groups]
+    n_streams = sum(n + 2 for n in npg)
+    rng = np.frombuffer(d.rng_streams(n_streams, w["seed"]), dtype="<u8")
+    t0 = time.perf_counter()
+    port.filter_run("sir_cases", pars, npg, 0.0, w["times"], data.ravel(),
+                    n_groups, w["dt"], rng, n_runs=n_runs, n_state=4,
+                    n_threads=n_threads)
+    dt = (time.perf_counter() - t0) / n_runs
+    ps = sum(npg) * w["times"].size * STEPS_PER_OBS
+    return dt, ps
+
+
+def cpu_baseline(w, target_seconds):
+    from oracle import pyoracle
+    port = pyoracle.port()
+    threads = port.max_threads()
+    # calibrate on the first group, then grow the sample to the target
+    t1, ps1 = run_cpu(w, 1, threads)
+    rate = ps1 / max(t1, 1e-9)
+    G = len(w["n_particles"])
+    n_groups = 1
+    total = ps1
+    per_group = [n * w["times"].size * STEPS_PER_OBS for n in w["n_particles"]]
+    while n_groups < G and total / rate < target_seconds:
+        total += per_group[n_groups]
+        n_groups += 1
+    t, ps = run_cpu(w, n_groups, threads)
+    sample = (f"groups 1-{n_groups} of {G} ({sum(w['n_particles'][:n_groups])}"
+              f" particles), all {w['times'].size} observations, one "
+              "likelihood evaluation")
+    return {"value": ps / t, "unit": "particle-steps/s", "cores": threads,
+            "kind": "port", "sample": sample, "seconds": t}
+
+
+def gpu_simulate_factory():
+    import dust2_gb300 as d
+    from dust2_gb300 import _lib
+
+    def simulate(name, flat, n_groups, n_particles, dt, seed, times):
+        import ctypes
+        flat = _lib.as_f64(flat)
+        times = _lib.as_f64(times)
+        words = np.array([seed], dtype=np.uint64)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().dust2_gb300_system_alloc(
+            name.encode(), _lib.dptr(flat), n_groups, n_particles, 0.0, dt,
+            None, _lib.uptr(words), 1, 0, ctypes.byref(h)))
+        try:
+            _lib.check(_lib.lib().dust2_gb300_system_set_state_initial(h))
+            n_state = {"sir_cases": 4, "sir": 5}[name]
+            out = np.empty(times.size * n_groups * n_particles * n_state)
+            _lib.check(_lib.lib().dust2_gb300_system_simulate(
+                h, _lib.dptr(times), times.size, None, 0, _lib.dptr(out)))
+        finally:
+            _lib.lib().dust2_gb300_system_free(h)
+        return out
+    return simulate
+
+
+def gpu_arm(args, rank, world, local):
+    import ctypes
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else
+                                "gloo")
+    import __graft_entry__
+    __graft_entry__.build()
+    import dust2_gb300 as d
+    from dust2_gb300 import _lib
+
+    w = build_workload(args.workload, gpu_simulate_factory())
+    gen = d.sir_cases()
+    npg = w["n_particles"]
+    obj = d.dust_filter_create(gen, 0, data_columns(w),
+                               n_particles=npg if len(npg) > 1 else npg[0],
+                               dt=w["dt"], seed=w["seed"])
+    plist = w["plist"] if len(npg) > 1 else w["plist"][0]
+    d.dust_likelihood_run(obj, plist)  # allocate and initialise
+    lib = _lib.lib()
+    h = obj.ptr
+    n_total = sum(npg)
+    n_obs = w["times"].size
+    n_groups = len(npg)
+    particle_steps = n_total * n_obs * STEPS_PER_OBS
+    ll = np.empty(n_groups)
+
+    stream_ptr = ctypes.c_void_p()
+    _lib.check(lib.dust2_gb300_filter_stream(h, ctypes.byref(stream_ptr)))
+    ext = torch.cuda.ExternalStream(stream_ptr.value)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def run_once():
+        _lib.check(lib.dust2_gb300_filter_run_async(h, None, 0))
+
+    for _ in range(args.warmup):
+        run_once()
+        _lib.check(lib.dust2_gb300_filter_last_log_likelihood(h,
+                                                              _lib.dptr(ll)))
+    _lib.check(lib.dust2_gb300_filter_set_timing(h, 1))
+    run_once()  # capture the timed graph outside the timed region
+    _lib.check(lib.dust2_gb300_filter_last_log_likelihood(h, _lib.dptr(ll)))
+    _lib.check(lib.dust2_gb300_filter_set_timing(h, 1))
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    elapsed = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        run_once()
+        e1.record(ext)
+        _lib.check(lib.dust2_gb300_filter_last_log_likelihood(
+            h, _lib.dptr(ll)))
+        elapsed.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clock_info = clocks.stop()
+    step_ms = ctypes.c_double()
+    run_ms = ctypes.c_double()
+    n_step = ctypes.c_int64()
+    n_run = ctypes.c_int64()
+    _lib.check(lib.dust2_gb300_filter_kernel_times(
+        h, ctypes.byref(step_ms), ctypes.byref(n_step), ctypes.byref(run_ms),
+        ctypes.byref(n_run)))
+    _lib.check(lib.dust2_gb300_filter_set_timing(h, 0))
+    ms = float(np.mean(elapsed))
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = particle_steps * world / (ms_max * 1e-3)
+
+    # end to end through the public API: host parameters in, host
+    # log-likelihoods out, every step
+    e2e_times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = d.dust_likelihood_run(obj, plist)
+        e2e_times.append(time.perf_counter() - t0)
+    assert np.all(np.isfinite(res))
+    e2e_s = float(np.mean(e2e_times))
+    e2e_max = e2e_s
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_max = float(t.item())
+    h2d = n_groups * gen.n_pars * 8
+    d2h = n_groups * 8 + n_groups * 4 + 4
+
+    step_launch_ms = step_ms.value / max(1, n_step.value)
+    roofline = None
+    if rank == 0:
+        peak = fp64_peak_tflops()
+        ps_per_launch = n_total * STEPS_PER_OBS
+        achieved = None
+        frac = None
+        if FP64_OPS_PER_PARTICLE_STEP is not None:
+            achieved = (FP64_OPS_PER_PARTICLE_STEP * ps_per_launch /
+                        (step_launch_ms * 1e-3) / 1e12)
+            frac = achieved / peak
+        roofline = {
+            "bound": "fp64", "kernel": "k_step_compare<sir_cases>",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": frac, "traffic": None,
+            "peak_source": "measured in-process: DFMA-chain microbenchmark "
+                           "(dust2_gb300_fp64_peak); MEASURED_PEAKS.json has no FP64 entry",
+            "step_launch_ms": step_launch_ms,
+            "step_share_of_run": step_ms.value / max(run_ms.value, 1e-12),
+            "flops_basis": "executed FP64 ops per particle-step (ncu SASS "
+                           "dadd+dmul+2*dfma)"}
+
+    if rank == 0:
+        line = {
+            "metric": "filter particle-steps/s",
+            "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (simulated by the model, seeded)",
+            "config": {"workload": args.workload, "n_groups": n_groups,
+                       "n_particles_total": n_total, "n_observations": n_obs,
+                       "steps_per_observation": STEPS_PER_OBS,
+                       "particle_steps_per_step": particle_steps,
+                       "l2": "flushed (256 MB write) between timed steps",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": particle_steps * world / e2e_max,
+                    "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_max},
+            "gpu_launches": args.steps * (2 + 6 * n_obs),
+            "clocks": clock_info,
+            "roofline": roofline,
+            "serial_fallbacks": d.dust_likelihood_serial_fallbacks(obj),
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def reference_arm(args, rank, world):
+    """The CPU implementation of the path on the host cores (the oracle
+    port of dust2's engine; dust2's own sources are not present on the
+    benchmark machine)."""
+    if rank != 0:
+        return
+    import __graft_entry__  # noqa: F401
+    from oracle import build as oracle_build
+    oracle_build.build_port()
+    from dust2_gb300 import build as engine_build
+    engine_build.build()
+    from oracle import pyoracle
+
+    w = build_workload(args.workload, oracle_simulate())
+    port = pyoracle.port()
+    threads = port.max_threads()
+    base = cpu_baseline(w, args.cpu_seconds)
+    n_groups = int(base["sample"].split("-")[1].split(" ")[0])
+    for _ in range(args.warmup):
+        run_cpu(w, n_groups, threads)
+    times = []
+    ps = None
+    for _ in range(args.steps):
+        t, ps = run_cpu(w, n_groups, threads)
+        times.append(t)
+    t = float(np.mean(times))
+    value = ps / t
+    line = {
+        "impl": "reference", "metric": "filter particle-steps/s",
+        "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (simulated by the model, seeded)",
+        "config": {"workload": args.workload},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s",
+                         "cores": threads, "kind": "port",
+                         "sample": base["sample"]},
+        "e2e": {"value": value, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def oracle_simulate():
+    from oracle import pyoracle
+
+    def simulate(name, flat, n_groups, n_particles, dt, seed, times):
+        import dust2_gb300 as d
+        rng = np.frombuffer(d.rng_streams(n_groups * n_particles, seed),
+                            dtype="<u8")
+        out, _ = pyoracle.port().discrete_simulate(
+            name, flat, n_groups, n_particles, 0.0, dt, rng, times)
+        n_state = {"sir_cases": 4, "sir": 5}[name]
+        return out[:times.size * n_groups * n_particles * n_state]
+    return simulate
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_info()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

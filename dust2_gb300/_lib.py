@@ -47,6 +47,7 @@ _SIGNATURES = {
     "dust2_gb300_device_count": (ctypes.c_int,
                                  [ctypes.POINTER(ctypes.c_int32)]),
     "dust2_gb300_systems": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "dust2_gb300_fp64_peak": (ctypes.c_int, [c_double_p]),
     "dust2_gb300_system_info": (ctypes.c_int, [ctypes.c_char_p,
                                                ctypes.c_char_p,
                                                ctypes.c_size_t]),
@@ -113,6 +114,16 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_int32, c_double_p]),
     "dust2_gb300_filter_serial_fallbacks": (ctypes.c_int, [
         ctypes.c_void_p, c_i64_p]),
+    "dust2_gb300_filter_run_async": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, ctypes.c_size_t]),
+    "dust2_gb300_filter_last_log_likelihood": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p]),
+    "dust2_gb300_filter_stream": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "dust2_gb300_filter_set_timing": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32]),
+    "dust2_gb300_filter_kernel_times": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, c_i64_p, c_double_p, c_i64_p]),
 }
 
 _lib = None

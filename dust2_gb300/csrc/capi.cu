@@ -696,4 +696,42 @@ int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,
   return guard([&] { *n = filref(filter).n_serial_fallbacks(); });
 }
 
+int dust2_gb300_filter_run_async(dust2_gb300_filter* filter,
+                                 const size_t* index_group,
+                                 size_t n_index_group) {
+  return guard([&] {
+    auto& f = filref(filter);
+    auto ig = to_int_index(index_group, n_index_group, f.sys().n_groups(),
+                           "index_group");
+    f.run_async(ig.empty() ? nullptr : ig.data(),
+                static_cast<int>(ig.size()));
+    filter->last_index_group = ig;
+  });
+}
+
+int dust2_gb300_filter_last_log_likelihood(dust2_gb300_filter* filter,
+                                           double* ll) {
+  return guard([&] { filref(filter).last_log_likelihood(ll); });
+}
+
+int dust2_gb300_filter_stream(dust2_gb300_filter* filter, void** stream) {
+  return guard([&] { *stream = filref(filter).stream_handle(); });
+}
+
+int dust2_gb300_filter_set_timing(dust2_gb300_filter* filter,
+                                  int32_t enable) {
+  return guard([&] { filref(filter).set_timing(enable != 0); });
+}
+
+int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
+                                    double* step_ms, int64_t* n_step_launches,
+                                    double* run_ms, int64_t* n_runs) {
+  return guard([&] {
+    long a = 0, b = 0;
+    filref(filter).kernel_times(step_ms, &a, run_ms, &b);
+    *n_step_launches = a;
+    *n_runs = b;
+  });
+}
+
 }  // extern "C"

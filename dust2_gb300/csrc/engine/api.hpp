@@ -118,6 +118,16 @@ public:
   virtual long n_serial_fallbacks() const = 0;
   // Run options.
   virtual void set_use_graph(bool use) = 0;
+  // Enqueue a run on the filter's stream without waiting; the
+  // log-likelihood stays on the device until last_log_likelihood().
+  virtual void run_async(const int* index_group, int n_index_group) = 0;
+  virtual void last_log_likelihood(double* ll_out) = 0;
+  virtual void* stream_handle() = 0;
+  // Record CUDA events around every step kernel (inside the graph) and
+  // accumulate their device time.
+  virtual void set_timing(bool enable) = 0;
+  virtual void kernel_times(double* step_ms, long* n_step_launches,
+                            double* run_ms, long* n_runs) = 0;
 };
 
 }  // namespace engine

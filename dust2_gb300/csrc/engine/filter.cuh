@@ -267,26 +267,89 @@ public:
 
   void run(const double* initial, const int* index_group, int n_index_group,
            double* ll_out) override {
+    launch(initial, index_group, n_index_group);
+    std::vector<double> ll(sys_->layout().n_groups);
+    finish(ll.data());
+    if (index_group == nullptr) {
+      std::copy(ll.begin(), ll.end(), ll_out);
+    } else {
+      for (int i = 0; i < n_index_group; ++i) {
+        ll_out[i] = ll[index_group[i]];
+      }
+    }
+  }
+
+  void run_async(const int* index_group, int n_index_group) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    launch(nullptr, index_group, n_index_group);
+  }
+
+  void last_log_likelihood(double* ll_out) override {
+    if (pending_) {
+      finish(ll_out);
+    } else {
+      DUST2_CUDA(cudaMemcpy(ll_out, ll_.data(),
+                            sys_->layout().n_groups * sizeof(double),
+                            cudaMemcpyDeviceToHost));
+    }
+  }
+
+  void* stream_handle() override {
+    return static_cast<void*>(sys_->stream());
+  }
+
+  void set_timing(bool enable) override {
+    if (enable != timing_) {
+      if (pending_) {
+        finish(nullptr);
+      }
+      timing_ = enable;
+      graph_state_ptr_ = nullptr;  // force a re-capture
+    }
+    step_ms_ = 0;
+    run_ms_ = 0;
+    n_step_launches_ = 0;
+    n_timed_runs_ = 0;
+  }
+
+  void kernel_times(double* step_ms, long* n_step_launches, double* run_ms,
+                    long* n_runs) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    *step_ms = step_ms_;
+    *n_step_launches = n_step_launches_;
+    *run_ms = run_ms_;
+    *n_runs = n_timed_runs_;
+  }
+
+  // Enqueue one run: reset (filter.hpp:156-175) then the observation loop.
+  void launch(const double* initial, const int* index_group,
+              int n_index_group) {
     auto& S = *sys_;
     const auto& L = S.layout();
     const int G = L.n_groups;
     auto s = S.stream();
-    std::vector<int> active(G, index_group == nullptr ? 1 : 0);
+    if (pending_) {
+      finish(nullptr);
+    }
+    active_host_.assign(G, index_group == nullptr ? 1 : 0);
     if (index_group != nullptr) {
       for (int i = 0; i < n_index_group; ++i) {
-        active[index_group[i]] = 1;
+        active_host_[index_group[i]] = 1;
       }
     }
-    // reset(): errors, time and (optionally) state (filter.hpp:156-175)
     S.reset_errors();
     S.set_time(time_start_);
     if (initial != nullptr) {
       S.put_state(initial);
     }
-    const int set_initial = initial == nullptr ? 1 : 0;
-    DUST2_CUDA(cudaMemcpyAsync(active_.data(), active.data(), G * sizeof(int),
-                               cudaMemcpyHostToDevice, s));
-    DUST2_CUDA(cudaMemcpyAsync(set_initial_.data(), &set_initial,
+    set_initial_host_ = initial == nullptr ? 1 : 0;
+    DUST2_CUDA(cudaMemcpyAsync(active_.data(), active_host_.data(),
+                               G * sizeof(int), cudaMemcpyHostToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(set_initial_.data(), &set_initial_host_,
                                sizeof(int), cudaMemcpyHostToDevice, s));
     if (use_graph_) {
       if (graph_exec_ == nullptr || graph_state_ptr_ != S.state_ptr()) {
@@ -296,26 +359,31 @@ public:
     } else {
       enqueue();
     }
-    std::vector<double> ll(G);
-    DUST2_CUDA(cudaMemcpyAsync(ll.data(), ll_.data(), G * sizeof(double),
-                               cudaMemcpyDeviceToHost, s));
-    std::vector<int> flags(G);
-    DUST2_CUDA(cudaMemcpyAsync(flags.data(), fallback_count_.data(),
+    pending_ = true;
+  }
+
+  // Wait for the last launched run; copy its log-likelihoods (all
+  // groups) to ll_out when given; raise any particle errors.
+  void finish(double* ll_out) {
+    auto& S = *sys_;
+    const int G = S.layout().n_groups;
+    auto s = S.stream();
+    pending_ = false;
+    fallback_host_.resize(G);
+    if (ll_out != nullptr) {
+      DUST2_CUDA(cudaMemcpyAsync(ll_out, ll_.data(), G * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+    }
+    DUST2_CUDA(cudaMemcpyAsync(fallback_host_.data(), fallback_count_.data(),
                                G * sizeof(int), cudaMemcpyDeviceToHost, s));
     S.check_errors_after();
     for (int g = 0; g < G; ++g) {
-      n_fallbacks_ += flags[g];
+      n_fallbacks_ += fallback_host_[g];
+    }
+    if (timing_) {
+      accumulate_timing();
     }
     S.set_time(schedule_.empty() ? time_start_ : schedule_.back().t_compare);
-    if (index_group == nullptr) {
-      for (int g = 0; g < G; ++g) {
-        ll_out[g] = ll[g];
-      }
-    } else {
-      for (int i = 0; i < n_index_group; ++i) {
-        ll_out[i] = ll[index_group[i]];
-      }
-    }
     random_particle_.assign(G, -1);
     has_run_ = true;
   }
@@ -407,6 +475,13 @@ public:
   }
 
   ~filter_engine() override {
+    cudaStreamSynchronize(sys_->stream());
+    for (auto e : ev_step_) {
+      cudaEventDestroy(e);
+    }
+    for (auto e : ev_run_) {
+      cudaEventDestroy(e);
+    }
     if (graph_exec_ != nullptr) {
       cudaGraphExecDestroy(graph_exec_);
     }
@@ -430,6 +505,10 @@ private:
     }
     filter_view f = view();
     f.gflag = gflag_.data();
+    if (timing_) {
+      ensure_events();
+      record(ev_run_[0]);
+    }
     k_filter_reset<<<n_blocks(G, 128), 128, 0, s>>>(f, G);
     DUST2_CUDA(cudaMemsetAsync(fallback_count_.data(), 0, G * sizeof(int), s));
     system_view<T> v = S.view();
@@ -440,9 +519,15 @@ private:
     for (std::size_t i = 0; i < schedule_.size(); ++i) {
       const auto& st = schedule_[i];
       v.state = cur;
+      if (timing_) {
+        record(ev_step_[2 * i]);
+      }
       k_step_compare<T><<<NT, TS, 0, s>>>(
         v, f, st.t0, S.dt(), st.n_steps, st.t_compare,
         data_.data() + i * n_groups_data_, n_groups_data_);
+      if (timing_) {
+        record(ev_step_[2 * i + 1]);
+      }
       k_weights<<<NT, TS, 0, s>>>(f);
       k_group<<<G, 32, 0, s>>>(f, G);
       k_resample<<<NT, TS, 0, s>>>(f);
@@ -458,7 +543,44 @@ private:
                                  L.stride * sizeof(double),
                                  cudaMemcpyDeviceToDevice, s));
     }
+    if (timing_) {
+      record(ev_run_[1]);
+    }
     DUST2_CUDA(cudaGetLastError());
+  }
+
+  void ensure_events() {
+    const std::size_t need = 2 * schedule_.size();
+    while (ev_step_.size() < need) {
+      cudaEvent_t e;
+      DUST2_CUDA(cudaEventCreate(&e));
+      ev_step_.push_back(e);
+    }
+    while (ev_run_.size() < 2) {
+      cudaEvent_t e;
+      DUST2_CUDA(cudaEventCreate(&e));
+      ev_run_.push_back(e);
+    }
+  }
+
+  void record(cudaEvent_t e) {
+    DUST2_CUDA(cudaEventRecordWithFlags(
+      e, sys_->stream(), capturing_ ? cudaEventRecordExternal :
+      cudaEventRecordDefault));
+  }
+
+  void accumulate_timing() {
+    for (std::size_t i = 0; i < schedule_.size(); ++i) {
+      float ms = 0;
+      DUST2_CUDA(cudaEventElapsedTime(&ms, ev_step_[2 * i],
+                                      ev_step_[2 * i + 1]));
+      step_ms_ += ms;
+      n_step_launches_++;
+    }
+    float ms = 0;
+    DUST2_CUDA(cudaEventElapsedTime(&ms, ev_run_[0], ev_run_[1]));
+    run_ms_ += ms;
+    n_timed_runs_++;
   }
 
   void k_fallback_counted(filter_view f, cudaStream_t s);
@@ -474,16 +596,19 @@ private:
       graph_ = nullptr;
     }
     DUST2_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    capturing_ = true;
     try {
       enqueue();
     } catch (...) {
-      cudaGraph_t g;
+      capturing_ = false;
+      cudaGraph_t g = nullptr;
       cudaStreamEndCapture(s, &g);
       if (g != nullptr) {
         cudaGraphDestroy(g);
       }
       throw;
     }
+    capturing_ = false;
     DUST2_CUDA(cudaStreamEndCapture(s, &graph_));
     DUST2_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
     graph_state_ptr_ = sys_->state_ptr();
@@ -497,7 +622,19 @@ private:
   std::vector<int> random_particle_;
   bool has_run_ = false;
   bool use_graph_ = true;
+  bool pending_ = false;
+  bool capturing_ = false;
+  bool timing_ = false;
   long n_fallbacks_ = 0;
+  std::vector<int> active_host_;
+  int set_initial_host_ = 1;
+  std::vector<int> fallback_host_;
+  std::vector<cudaEvent_t> ev_step_;
+  std::vector<cudaEvent_t> ev_run_;
+  double step_ms_ = 0;
+  double run_ms_ = 0;
+  long n_step_launches_ = 0;
+  long n_timed_runs_ = 0;
 
   device_array<int> active_, n_part_, offset_, tile_first_, tile_count_;
   device_array<double> w_, ew_, pre_, tile_sum_, tile_off_;

@@ -1,0 +1,86 @@
+"""Synthetic inputs of the benchmark workloads (no external datasets).
+
+Each builder takes a `simulate` callable, so the same recipe runs on the
+CUDA engine (benchmarks) and on the CPU oracle (test fixtures):
+    simulate(name, flat_pars, n_groups, n_particles, dt, seed, times)
+      -> array [n_times][group][particle][state]
+Parameter packing uses the system's parameter table from the library.
+"""
+
+import math
+
+import numpy as np
+
+from .interface import Generator
+
+
+def pack(name, plist):
+    gen = Generator(name)
+    return np.concatenate([gen.pack_pars(p) for p in plist])
+
+
+def sir_small(simulate):
+    """Single-group SIR filter: N=1000, I0=10, beta=0.2, gamma=0.1,
+    dt=0.25, 1000 particles, 100 daily observations simulated by the same
+    model from seed 42 plus Poisson observation noise."""
+    p = {"N": 1000, "I0": 10, "beta": 0.2, "gamma": 0.1}
+    flat = pack("sir_cases", [p])
+    times = np.arange(1, 101, dtype=float)
+    sim = simulate("sir_cases", flat, 1, 1, 0.25, 42, times)
+    cases = np.asarray(sim).reshape(times.size, 4)[:, 3]
+    rs = np.random.default_rng(42)
+    data = rs.poisson(cases + 1e-6).astype(float)
+    return {"pars": flat, "plist": [p], "times": times, "data": data,
+            "dt": 0.25, "n_particles": 1000, "seed": 42}
+
+
+def sir_batched(simulate, n_groups=64, seed=1, n_obs=200):
+    """Batched SIR filter: 64 groups with beta ~ U(0.1, 0.5), gamma ~
+    U(0.05, 0.2), N = 1e6, I0 ~ U{1..100}; particle counts
+    round(2^U(9, 15)); 200 daily observations per group simulated from
+    seed 1 plus Poisson noise."""
+    rs = np.random.default_rng(seed)
+    plist = []
+    for _ in range(n_groups):
+        plist.append({"N": 1e6, "I0": float(rs.integers(1, 101)),
+                      "beta": float(rs.uniform(0.1, 0.5)),
+                      "gamma": float(rs.uniform(0.05, 0.2))})
+    n_particles = [int(round(2 ** rs.uniform(9, 15))) for _ in range(n_groups)]
+    flat = pack("sir_cases", plist)
+    times = np.arange(1, n_obs + 1, dtype=float)
+    sim = simulate("sir_cases", flat, n_groups, 1, 0.25, seed, times)
+    cases = np.asarray(sim).reshape(times.size, n_groups, 4)[:, :, 3]
+    data = rs.poisson(cases + 1e-6).astype(float)  # [time][group]
+    return {"pars": flat, "plist": plist, "times": times, "data": data,
+            "dt": 0.25, "n_particles": n_particles, "seed": seed}
+
+
+def contact_matrix(seed=7, n_age=16):
+    """Random symmetric contact matrix, entries Gamma(2, 1) / 16."""
+    rs = np.random.default_rng(seed)
+    a = rs.gamma(2.0, 1.0, size=(n_age, n_age)) / 16
+    return np.triu(a) + np.triu(a, 1).T
+
+
+def seir_plist(r0_values, seed=7):
+    c = contact_matrix(seed)
+    return [{"R0": float(r), "sigma": 0.2, "gamma": 0.1, "size": 20,
+             "I0": 1, "contact": c.ravel()} for r in r0_values]
+
+
+def sirode_batched(n_instances=262144, seed=3):
+    """dopri5 workload: beta ~ U(0.1, 0.5), gamma ~ U(0.05, 0.2), N = 1e6,
+    I0 ~ U(1, 100); one parameter group per instance."""
+    rs = np.random.default_rng(seed)
+    beta = rs.uniform(0.1, 0.5, n_instances)
+    gamma = rs.uniform(0.05, 0.2, n_instances)
+    i0 = rs.uniform(1, 100, n_instances)
+    gen = Generator("sirode")
+    flat = np.empty((n_instances, gen.n_pars))
+    # parameter table order: I0, N, beta, gamma
+    flat[:, 0] = i0
+    flat[:, 1] = 1e6
+    flat[:, 2] = beta
+    flat[:, 3] = gamma
+    return {"pars": flat.ravel(), "n_groups": n_instances,
+            "times": np.arange(0, 201, dtype=float)}

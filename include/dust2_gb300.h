@@ -72,6 +72,11 @@ size_t dust2_gb300_last_error(char* buf, size_t len);
 /* Number of CUDA devices visible (0 without a GPU). */
 int dust2_gb300_device_count(int32_t* n);
 
+/* Measured FP64 FMA throughput of the current device in TFLOP/s
+ * (independent DFMA chains on every SM); the denominator of the
+ * FP64-pipe roofline.  No counterpart in dust2. */
+int dust2_gb300_fp64_peak(double* tflops);
+
 /* Names of the compiled-in systems, comma separated. */
 int dust2_gb300_systems(char* buf, size_t len);
 
@@ -249,6 +254,33 @@ int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
  * the exact-resampling check). */
 int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,
                                         int64_t* n);
+
+/* Asynchronous form of dust2_gb300_filter_run (system initial conditions,
+ * current parameters): enqueues the run on the filter's CUDA stream and
+ * returns; results stay on the device.  No counterpart in dust2, whose
+ * verbs are synchronous; it lets a caller keep several filters busy. */
+int dust2_gb300_filter_run_async(dust2_gb300_filter* filter,
+                                 const size_t* index_group,
+                                 size_t n_index_group);
+
+/* Wait for the last run and copy one log-likelihood per group (all
+ * groups) into ll; reports errors of an asynchronous run. */
+int dust2_gb300_filter_last_log_likelihood(dust2_gb300_filter* filter,
+                                           double* ll);
+
+/* The CUDA stream (cudaStream_t) the filter's work is issued on. */
+int dust2_gb300_filter_stream(dust2_gb300_filter* filter, void** stream);
+
+/* Enable (1) or disable (0) device timing of the filter's step kernels:
+ * CUDA events recorded around every step launch inside the captured
+ * graph.  Resets the accumulated times. */
+int dust2_gb300_filter_set_timing(dust2_gb300_filter* filter, int32_t enable);
+
+/* Accumulated device time of the step kernels (ms, number of launches)
+ * and of whole runs (ms, number of runs) since timing was enabled. */
+int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
+                                    double* step_ms, int64_t* n_step_launches,
+                                    double* run_ms, int64_t* n_runs);
 
 #ifdef __cplusplus
 }

@@ -923,6 +923,55 @@ int oracle_ode_simulate(const char* name, const double* pars, int n_groups,
   }
 }
 
+// The project's elementary functions evaluated on the host (fn: 0 exp,
+// 1 log, 2 lgamma, 3 cos(2 pi x), 4 sin(2 pi x)).
+void oracle_math(int fn, const double* x, int n, double* out) {
+  for (int i = 0; i < n; ++i) {
+    double s, c;
+    switch (fn) {
+    case 0: out[i] = dust2gpu::math::exp(x[i]); break;
+    case 1: out[i] = dust2gpu::math::log(x[i]); break;
+    case 2: out[i] = dust2gpu::math::lgamma(x[i]); break;
+    case 3: dust2gpu::math::sincos_2pi(x[i], &s, &c); out[i] = c; break;
+    default: dust2gpu::math::sincos_2pi(x[i], &s, &c); out[i] = s; break;
+    }
+  }
+}
+
+// n draws from one stream (dist: 0 binomial(a, b), 1 poisson(a),
+// 2 normal(a, b), 3 exponential_rate(a), 4 uniform(a, b),
+// 5 random_real); returns the error code of the generator.
+int oracle_draws(int dist, double a, double b, int n, const uint64_t* rng,
+                 double* out) {
+  auto r = make_rng(rng, 1, false)[0];
+  for (int i = 0; i < n; ++i) {
+    switch (dist) {
+    case 0: out[i] = dust2gpu::random::binomial(r, a, b); break;
+    case 1: out[i] = dust2gpu::random::poisson(r, a); break;
+    case 2: out[i] = dust2gpu::random::normal(r, a, b); break;
+    case 3: out[i] = dust2gpu::random::exponential_rate(r, a); break;
+    case 4: out[i] = dust2gpu::random::uniform(r, a, b); break;
+    default: out[i] = dust2gpu::random::random_real(r); break;
+    }
+  }
+  return r.err;
+}
+
+// log densities (dist: 0 poisson(x | a), 1 negative_binomial_mu(x | a, b),
+// 2 normal(x | a, b))
+void oracle_density(int dist, const double* x, int n, double a, double b,
+                    double* out) {
+  for (int i = 0; i < n; ++i) {
+    switch (dist) {
+    case 0: out[i] = dust2gpu::density::poisson(x[i], a, true); break;
+    case 1:
+      out[i] = dust2gpu::density::negative_binomial_mu(x[i], a, b, true);
+      break;
+    default: out[i] = dust2gpu::density::normal(x[i], a, b, true); break;
+    }
+  }
+}
+
 double oracle_scale_log_weights(int n, double* w) {
   return scale_log_weights(n, w);
 }

@@ -199,3 +199,42 @@ def ref():
                 return None
         _ref = Oracle(REF_LIB, "ref")
     return _ref
+
+
+def port_math(fn, x):
+    """The project's exp/log/lgamma/cos2pi/sin2pi evaluated on the host."""
+    o = port()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    f = o.lib.oracle_math
+    f.restype = None
+    code = {"exp": 0, "log": 1, "lgamma": 2, "cos2pi": 3, "sin2pi": 4}[fn]
+    f(ctypes.c_int(code), x.ctypes.data_as(_d), ctypes.c_int(x.size),
+      out.ctypes.data_as(_d))
+    return out
+
+
+def port_draws(dist, a, b, n, rng):
+    """n draws of a sampler from one stream; returns (draws, error code)."""
+    o = port()
+    rng = np.ascontiguousarray(rng, dtype=np.uint64)
+    out = np.empty(n)
+    f = o.lib.oracle_draws
+    f.restype = ctypes.c_int
+    code = {"binomial": 0, "poisson": 1, "normal": 2, "exponential": 3,
+            "uniform": 4, "real": 5}[dist]
+    err = f(ctypes.c_int(code), ctypes.c_double(a), ctypes.c_double(b),
+            ctypes.c_int(n), rng.ctypes.data_as(_u), out.ctypes.data_as(_d))
+    return out, err
+
+
+def port_density(dist, x, a, b=0.0):
+    o = port()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    f = o.lib.oracle_density
+    f.restype = None
+    code = {"poisson": 0, "negbin": 1, "normal": 2}[dist]
+    f(ctypes.c_int(code), x.ctypes.data_as(_d), ctypes.c_int(x.size),
+      ctypes.c_double(a), ctypes.c_double(b), out.ctypes.data_as(_d))
+    return out

@@ -1,0 +1,145 @@
+"""Generate the golden fixtures in tests/golden/ from dust2's own engine.
+
+The reference engine (inst/include/dust2 compiled unmodified with the
+project's monty stand-in, oracle/ref_driver.cpp) is run on seeded
+synthetic inputs and its outputs are saved as .npz files.  The GPU tests
+compare the CUDA engine against these files on machines where the
+reference sources are absent.  Streams are generated by the independent
+numpy implementation in tests/xoshiro.py, so the fixtures do not depend
+on the engine under test.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+from oracle import pyoracle  # noqa: E402
+import xoshiro  # noqa: E402
+import workload_data  # noqa: E402
+from dust2_gb300 import workloads  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def save(name, **kw):
+    np.savez_compressed(OUT / f"{name}.npz", **kw)
+    print("wrote", name)
+
+
+def main():
+    ref = pyoracle.ref()
+    if ref is None:
+        raise SystemExit("the reference sources are needed to make fixtures")
+
+    # 1. The filter of tests/testthat/test-filter.R "can run particle
+    #    filter": sir, 100 particles, data at 4,8,12,16, dt = 1, 20 runs;
+    #    here with 2 groups (test-filter.R "nested particle filter").
+    pars = workload_data.sir_pars([
+        {"beta": 0.1, "gamma": 0.2, "N": 1000, "I0": 10, "exp_noise": 1e6},
+        {"beta": 0.2, "gamma": 0.2, "N": 1000, "I0": 10, "exp_noise": 1e6}])
+    n = 100
+    rng = xoshiro.streams(42, 2 * (n + 2))
+    times = np.array([4.0, 8, 12, 16])
+    data = np.array([1.0, 2, 2, 3, 3, 4, 4, 5])
+    ll, state, rng_out = ref.filter_run("sir", pars, [n, n], 0.0, times, data,
+                                        2, 1.0, rng, n_runs=20, n_state=5)
+    save("filter_sir_2groups", pars=pars, n_particles=n, rng=rng,
+         times=times, data=data, dt=1.0, ll=ll, state=state[:2 * n * 5],
+         rng_out=rng_out)
+
+    # 2. Missing data in one group only (test-filter.R:470-515).
+    data_na = np.array([1.0, 2, 2, np.nan, np.nan, 4, np.nan, np.nan, 5, 6])
+    times5 = np.array([4.0, 8, 12, 16, 20])
+    ll, state, rng_out = ref.filter_run("sir", pars, [n, n], 0.0, times5,
+                                        data_na, 2, 1.0, rng, n_runs=5,
+                                        n_state=5)
+    save("filter_sir_missing", pars=pars, n_particles=n, rng=rng,
+         times=times5, data=data_na, dt=1.0, ll=ll, state=state[:2 * n * 5],
+         rng_out=rng_out)
+
+    # 3. The single-group SIR filter workload: 1000 particles, 100 daily
+    #    observations, dt = 0.25, data from the model at seed 42 plus
+    #    Poisson noise.
+    w = workload_data.sir_small(ref)
+    rng = xoshiro.streams(w["seed"], w["n_particles"] + 2)
+    ll, state, rng_out = ref.filter_run(
+        "sir_cases", w["pars"], [w["n_particles"]], 0.0, w["times"],
+        w["data"], 1, w["dt"], rng, n_runs=3, n_state=4)
+    save("filter_sir_cases_1000", pars=w["pars"],
+         n_particles=w["n_particles"], rng=rng, times=w["times"],
+         data=w["data"], dt=w["dt"], ll=ll,
+         state=state[:w["n_particles"] * 4], rng_out=rng_out)
+
+    # 4. Plain stepping (dust_system_run_to_time / simulate) of each
+    #    discrete system, 3 groups x 7 particles.
+    for name, plist, dt, tmax in [
+            ("sir", [{"beta": 0.3, "gamma": 0.1, "N": 1000, "I0": 10,
+                      "exp_noise": 1e6}] * 3, 0.25, 30),
+            ("walk", [{"sd": 1.0, "len": 3, "random_initial": 1},
+                      {"sd": 2.0, "len": 3, "random_initial": 1},
+                      {"sd": 3.0, "len": 3, "random_initial": 1}], 0.5, 10),
+            ("seir_age", workloads.seir_plist([1.5, 2.0, 2.5]), 0.25, 20)]:
+        flat = workload_data.pack(name, plist)
+        G, np_ = 3, 7
+        rng = xoshiro.streams(7, G * np_)
+        tt = np.arange(0, tmax + 1, dtype=float)
+        sim, rng_out = ref.discrete_simulate(name, flat, G, np_, 0.0, dt, rng,
+                                             tt)
+        n_state = {"sir": 5, "walk": 3, "seir_age": 96}[name]
+        save(f"simulate_{name}", pars=flat, n_groups=G, n_particles=np_,
+             rng=rng, dt=dt, times=tt,
+             out=sim[:tt.size * G * np_ * n_state], rng_out=rng_out)
+
+    # 5. compare_data of sir with exponential noise (test-sir.R:31-46).
+    flat = workload_data.pack("sir", [{"exp_noise": 0.5}])
+    rs = np.random.default_rng(3)
+    st = np.zeros((10, 5))
+    st[:, 4] = rs.poisson(30, 10)
+    rng = xoshiro.streams(42, 10)
+    out, rng_out = ref.compare("sir", flat, 1, 10, 0.0, st.ravel(),
+                               np.array([30.0]), 1, rng)
+    save("compare_sir", pars=flat, state=st.ravel(), rng=rng, out=out,
+         rng_out=rng_out)
+
+    # 6. dopri5: sirode and logistic.
+    flat = workload_data.pack("sirode", [
+        {"beta": 0.2, "gamma": 0.1, "N": 1000, "I0": 10},
+        {"beta": 0.4, "gamma": 0.05, "N": 1e6, "I0": 50}])
+    tt = np.arange(0, 201, dtype=float)
+    out, stats = ref.ode_simulate("sirode", flat, 2, 2, 0.0, tt, 5)
+    save("ode_sirode", pars=flat, times=tt, out=out, stats=stats)
+    flat = workload_data.pack("logistic", [
+        {"n": 3, "r": [0.1, 0.2, 0.3], "K": [100, 100, 100]}])
+    tt = np.arange(0, 51, dtype=float)
+    out, stats = ref.ode_simulate("logistic", flat, 1, 1, 0.0, tt, 4)
+    save("ode_logistic", pars=flat, times=tt, out=out, stats=stats)
+    out, stats = ref.ode_simulate("sirode", workload_data.pack(
+        "sirode", [{"beta": 0.2, "gamma": 0.1, "N": 1000, "I0": 10}]),
+        1, 1, 0.0, np.array([0.0, 50.0]), 5, critical_times=[10, 20, 30])
+    save("ode_sirode_critical", out=out, stats=stats)
+
+    # 7. Systematic resampling and log-weight scaling helpers
+    #    (test-filter-details.R:1-64).
+    rs = np.random.default_rng(1)
+    w = np.abs(rs.standard_cauchy(20))
+    u = rs.uniform()
+    cases = {"w": w, "u": np.array([u, 0.0, 1 - 1e-8])}
+    cases["idx"] = np.stack([ref.resample_weight(w, uu) for uu in cases["u"]])
+    lw = np.log(rs.uniform(size=50)) * 10
+    lw[[3, 17]] = np.nan
+    r1, w1 = ref.scale_log_weights(lw)
+    r2, w2 = ref.scale_log_weights(np.full(5, -np.inf))
+    r3, w3 = ref.scale_log_weights(np.array([-3.5]))
+    save("filter_details", **cases, lw=lw, lw_ret=np.array([r1, r2, r3]),
+         lw_w1=w1, lw_w2=w2, lw_w3=w3)
+
+
+if __name__ == "__main__":
+    main()
