@@ -165,6 +165,11 @@ def _check_dt(dt, generator):
     return dt
 
 
+def _fmod(n, m):
+    """dust2's own remainder (R/util.R:114-116), not C fmod."""
+    return np.floor(np.asarray(n) / m) * m - np.asarray(n)
+
+
 def _check_time(time, dt, name="time"):
     if np.ndim(time) != 0:
         raise DustError(f"'{name}' must be a scalar")
@@ -172,7 +177,7 @@ def _check_time(time, dt, name="time"):
         raise DustError(f"Expected '{name}' to be numeric")
     time = float(time)
     if dt is not None and dt > 0:
-        if abs(math.fmod(time, dt)) > math.sqrt(np.finfo(float).eps):
+        if abs(_fmod(time, dt)) > math.sqrt(np.finfo(float).eps):
             if dt == 1:
                 raise DustError(
                     f"'{name}' must be integer-like, because 'dt' is 1")
@@ -528,7 +533,7 @@ def _check_times(times, dt, name="times"):
             msg += f"\n...and {bad.size - 4} other errors"
         raise DustError(msg)
     if dt is not None and dt <= 1:
-        rem = np.fmod(times, dt)
+        rem = _fmod(times, dt)
         bad = np.nonzero(np.abs(rem) > math.sqrt(np.finfo(float).eps))[0]
         if bad.size:
             if dt == 1:

@@ -1,0 +1,188 @@
+"""The CPU oracle pinned to dust2's own engine.
+
+Where the reference sources are present, the CPU restatement
+(oracle/port) is checked bit for bit against dust2's engine compiled from
+those sources (oracle/ref_driver.cpp).  Everywhere, the restatement is
+checked against the golden fixtures that engine produced
+(tests/golden/make_golden.py)."""
+
+import numpy as np
+import pytest
+
+import xoshiro
+import workload_data
+from conftest import golden
+
+
+def test_port_filter_matches_golden(port):
+    for name in ("filter_sir_2groups", "filter_sir_missing"):
+        g = golden(name)
+        n = int(g["n_particles"])
+        ll, state, rng = port.filter_run(
+            "sir", g["pars"], [n, n], 0.0, g["times"], g["data"], 2,
+            float(g["dt"]), g["rng"], n_runs=g["ll"].shape[0], n_state=5)
+        np.testing.assert_array_equal(ll, g["ll"])
+        np.testing.assert_array_equal(state[:2 * n * 5], g["state"])
+        np.testing.assert_array_equal(rng, g["rng_out"])
+
+
+def test_port_single_group_workload_matches_golden(port):
+    g = golden("filter_sir_cases_1000")
+    n = int(g["n_particles"])
+    ll, state, rng = port.filter_run("sir_cases", g["pars"], [n], 0.0,
+                                     g["times"], g["data"], 1, float(g["dt"]),
+                                     g["rng"], n_runs=g["ll"].shape[0],
+                                     n_state=4)
+    np.testing.assert_array_equal(ll, g["ll"])
+    np.testing.assert_array_equal(state[:n * 4], g["state"])
+    np.testing.assert_array_equal(rng, g["rng_out"])
+
+
+@pytest.mark.parametrize("name", ["sir", "walk", "seir_age"])
+def test_port_simulate_matches_golden(port, name):
+    g = golden(f"simulate_{name}")
+    out, rng = port.discrete_simulate(name, g["pars"], int(g["n_groups"]),
+                                      int(g["n_particles"]), 0.0,
+                                      float(g["dt"]), g["rng"], g["times"])
+    np.testing.assert_array_equal(out[:g["out"].size], g["out"])
+    np.testing.assert_array_equal(rng, g["rng_out"])
+
+
+def test_port_compare_matches_golden(port):
+    g = golden("compare_sir")
+    out, rng = port.compare("sir", g["pars"], 1, 10, 0.0, g["state"],
+                            np.array([30.0]), 1, g["rng"])
+    np.testing.assert_array_equal(out, g["out"])
+    np.testing.assert_array_equal(rng, g["rng_out"])
+
+
+def test_port_ode_matches_golden(port):
+    g = golden("ode_sirode")
+    out, stats = port.ode_simulate("sirode", g["pars"], 2, 2, 0.0,
+                                   g["times"], 5)
+    np.testing.assert_array_equal(out, g["out"])
+    np.testing.assert_array_equal(stats, g["stats"])
+    g = golden("ode_logistic")
+    out, stats = port.ode_simulate("logistic", g["pars"], 1, 1, 0.0,
+                                   g["times"], 4)
+    np.testing.assert_array_equal(out, g["out"])
+    g = golden("ode_sirode_critical")
+    out, stats = port.ode_simulate(
+        "sirode", workload_data.pack(
+            "sirode", [{"beta": 0.2, "gamma": 0.1, "N": 1000, "I0": 10}]),
+        1, 1, 0.0, np.array([0.0, 50.0]), 5, critical_times=[10, 20, 30])
+    np.testing.assert_array_equal(out, g["out"])
+
+
+def test_port_details_match_golden(port):
+    g = golden("filter_details")
+    for u, idx in zip(g["u"], g["idx"]):
+        np.testing.assert_array_equal(port.resample_weight(g["w"], u), idx)
+    r1, w1 = port.scale_log_weights(g["lw"])
+    assert r1 == g["lw_ret"][0]
+    np.testing.assert_array_equal(w1, g["lw_w1"])
+    r2, w2 = port.scale_log_weights(np.full(5, -np.inf))
+    assert r2 == g["lw_ret"][1] == -np.inf
+    np.testing.assert_array_equal(w2, g["lw_w2"])
+    r3, w3 = port.scale_log_weights(np.array([-3.5]))
+    assert r3 == g["lw_ret"][2] == -3.5
+
+
+def test_resample_matches_find_interval(port):
+    """tests/testthat/test-filter-details.R:1-22: systematic resampling is
+    findInterval(u/n + (i-1)/n, cumsum(w/sum(w)))."""
+    rs = np.random.default_rng(1)
+    w = np.abs(rs.standard_cauchy(20))
+    for u in (rs.uniform(), 0.0, 1 - 1e-8):
+        n = w.size
+        uu = u / n + np.arange(n) / n
+        cw = np.cumsum(w / w.sum())
+        expect = np.searchsorted(cw, uu, side="right")
+        np.testing.assert_array_equal(port.resample_weight(w, u), expect)
+
+
+def test_scale_log_weights_semantics(port):
+    """test-filter-details.R:55-64: NaN -> zero weight; all -Inf -> -Inf."""
+    w = np.array([-1.0, np.nan, -2.0, -3.0])
+    r, ww = port.scale_log_weights(w)
+    m = -1.0
+    expect = np.log(np.mean(np.exp(np.array([-1.0, -2, -3]) - m)
+                            * np.array([1, 1, 1])) * 3 / 4) + m
+    assert abs(r - expect) < 1e-14
+    assert ww[1] == 0
+
+
+# ---- the restatement against dust2's own engine (reference present) ----
+
+def _uneven_inputs(seed, G, n, T):
+    rs = np.random.default_rng(seed)
+    plist = [{"N": 1e5, "I0": float(rs.integers(5, 50)),
+              "beta": float(rs.uniform(0.15, 0.5)),
+              "gamma": float(rs.uniform(0.05, 0.2))} for _ in range(G)]
+    times = np.arange(1, T + 1, dtype=float)
+    data = rs.poisson(20, size=(T, G)).astype(float)
+    data[rs.uniform(size=data.shape) < 0.05] = np.nan
+    return workload_data.pack("sir_cases", plist), times, data
+
+
+@pytest.mark.parametrize("G,n,dt", [(1, 1, 1.0), (3, 257, 0.25),
+                                    (2, 2000, 0.5)])
+def test_port_filter_equals_reference_engine(port, ref, G, n, dt):
+    pars, times, data = _uneven_inputs(G * n, G, n, 20)
+    rng = xoshiro.streams(G + n, G * (n + 2))
+    a = port.filter_run("sir_cases", pars, [n] * G, 0.0, times,
+                        data.ravel(), G, dt, rng, n_runs=3, n_state=4)
+    b = ref.filter_run("sir_cases", pars, [n] * G, 0.0, times, data.ravel(),
+                       G, dt, rng, n_runs=3, n_state=4)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1][:G * n * 4], b[1][:G * n * 4])
+    np.testing.assert_array_equal(a[2], b[2])
+
+
+def test_port_threads_do_not_change_results(port):
+    pars, times, data = _uneven_inputs(4, 3, 500, 15)
+    rng = xoshiro.streams(1, 3 * 502)
+    a = port.filter_run("sir_cases", pars, [500] * 3, 0.0, times,
+                        data.ravel(), 3, 0.25, rng, n_state=4, n_threads=1)
+    b = port.filter_run("sir_cases", pars, [500] * 3, 0.0, times,
+                        data.ravel(), 3, 0.25, rng, n_state=4,
+                        n_threads=port.max_threads())
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_port_seir_equals_reference_engine(port, ref):
+    from dust2_gb300 import workloads
+    pars = workload_data.pack("seir_age", workloads.seir_plist([1.5, 2.5]))
+    rng = xoshiro.streams(3, 2 * 5)
+    tt = np.arange(0, 31, dtype=float)
+    a = port.discrete_simulate("seir_age", pars, 2, 5, 0.0, 0.25, rng, tt)
+    b = ref.discrete_simulate("seir_age", pars, 2, 5, 0.0, 0.25, rng, tt)
+    np.testing.assert_array_equal(a[0][:tt.size * 10 * 96],
+                                  b[0][:tt.size * 10 * 96])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_port_ode_equals_reference_engine(port, ref):
+    rs = np.random.default_rng(2)
+    plist = [{"beta": float(rs.uniform(0.1, 0.5)),
+              "gamma": float(rs.uniform(0.05, 0.2)), "N": 1e6,
+              "I0": float(rs.uniform(1, 100))} for _ in range(20)]
+    pars = workload_data.pack("sirode", plist)
+    tt = np.arange(0, 201, dtype=float)
+    a = port.ode_simulate("sirode", pars, 20, 1, 0.0, tt, 5)
+    b = ref.ode_simulate("sirode", pars, 20, 1, 0.0, tt, 5)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+
+
+def test_port_errors_match_reference_engine(port, ref):
+    pars = workload_data.pack("sir", [{"gamma": -0.2}])
+    rng = xoshiro.streams(42, 10)
+    with pytest.raises(Exception) as e1:
+        port.discrete_simulate("sir", pars, 1, 10, 0.0, 1.0, rng, [30.0])
+    with pytest.raises(Exception) as e2:
+        ref.discrete_simulate("sir", pars, 1, 10, 0.0, 1.0, rng, [30.0])
+    assert str(e1.value) == str(e2.value)
+    assert str(e1.value).startswith("10 particles reported errors.")
+    assert "(and 6 more)" in str(e1.value)
