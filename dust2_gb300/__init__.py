@@ -13,8 +13,8 @@ from .interface import (
     dust_system_set_rng_state, dust_system_set_state,
     dust_system_set_state_initial, dust_system_set_time,
     dust_system_simulate, dust_system_state, dust_system_time,
-    dust_system_update_pars, logistic, rng_streams, seir_age, sir, sir_cases,
-    sirode, walk)
+    dust_system_update_pars, logistic, resample_weight, rng_streams,
+    scale_log_weights, seir_age, sir, sir_cases, sirode, walk)
 
 __all__ = [
     "DustError", "DustLikelihood", "DustSystem", "Generator",
@@ -27,5 +27,6 @@ __all__ = [
     "dust_system_run_to_time", "dust_system_set_rng_state",
     "dust_system_set_state", "dust_system_set_state_initial",
     "dust_system_set_time", "dust_system_simulate", "dust_system_state",
-    "dust_system_time", "dust_system_update_pars", "logistic", "rng_streams",
-    "seir_age", "sir", "sir_cases", "sirode", "walk"]
+    "dust_system_time", "dust_system_update_pars", "logistic",
+    "resample_weight", "rng_streams", "scale_log_weights", "seir_age", "sir",
+    "sir_cases", "sirode", "walk"]

@@ -114,6 +114,12 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_int32, c_double_p]),
     "dust2_gb300_filter_serial_fallbacks": (ctypes.c_int, [
         ctypes.c_void_p, c_i64_p]),
+    "dust2_gb300_resample_weight": (ctypes.c_int, [
+        c_double_p, ctypes.c_size_t, ctypes.c_double, c_size_p]),
+    "dust2_gb300_scale_log_weights": (ctypes.c_int, [
+        c_double_p, ctypes.c_size_t, c_double_p]),
+    "dust2_gb300_filter_set_serial_resample": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32]),
     "dust2_gb300_filter_run_async": (ctypes.c_int, [
         ctypes.c_void_p, c_size_p, ctypes.c_size_t]),
     "dust2_gb300_filter_last_log_likelihood": (ctypes.c_int, [

@@ -82,6 +82,14 @@ using dust2gpu::engine::system_api;
 
 thread_local std::string last_error;
 
+}  // namespace
+
+void dust2gpu::engine::set_last_error(const std::string& msg) {
+  last_error = msg;
+}
+
+namespace {
+
 template <typename F>
 int guard(F f) {
   try {
@@ -694,6 +702,11 @@ int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
 int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,
                                         int64_t* n) {
   return guard([&] { *n = filref(filter).n_serial_fallbacks(); });
+}
+
+int dust2_gb300_filter_set_serial_resample(dust2_gb300_filter* filter,
+                                           int32_t serial) {
+  return guard([&] { filref(filter).set_serial_resample(serial != 0); });
 }
 
 int dust2_gb300_filter_run_async(dust2_gb300_filter* filter,

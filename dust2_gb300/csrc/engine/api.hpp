@@ -21,6 +21,10 @@ std::string format_errors(const std::vector<particle_error>& errors,
                           std::size_t n_max = 4);
 std::string describe_error(const particle_error& e);
 
+// Set the calling thread's error message returned by
+// dust2_gb300_last_error (for entry points outside capi.cu).
+void set_last_error(const std::string& msg);
+
 struct ode_control {
   // inst/include/dust2/continuous/control.hpp:11-27; step_size_min is
   // clamped below by machine epsilon as in
@@ -118,6 +122,8 @@ public:
   virtual long n_serial_fallbacks() const = 0;
   // Run options.
   virtual void set_use_graph(bool use) = 0;
+  // Resample every group with the serial algorithm (verification mode).
+  virtual void set_serial_resample(bool serial) = 0;
   // Enqueue a run on the filter's stream without waiting; the
   // log-likelihood stays on the device until last_log_likelihood().
   virtual void run_async(const int* index_group, int n_index_group) = 0;

@@ -88,6 +88,7 @@ struct filter_view {
   int* idx;                   // [n_total] group-local source particle
   std::uint64_t* frng;        // [2 n_groups][4] filter streams
   int* set_initial;           // scalar flag read by the initial kernel
+  const int* force_serial;    // scalar flag: resample every group serially
 };
 
 __global__ void k_filter_reset(filter_view f, int n_groups);
@@ -217,6 +218,10 @@ public:
     idx_.resize(N);
     frng_.resize(8 * static_cast<std::size_t>(G));
     set_initial_.resize(1);
+    fallback_count_.resize(G);
+    force_serial_.resize(1);
+    DUST2_CUDA(cudaMemsetAsync(force_serial_.data(), 0, sizeof(int),
+                               sys_->stream()));
     data_.resize(data.size());
     auto s = sys_->stream();
     DUST2_CUDA(cudaMemcpyAsync(n_part_.data(), L.n_particles.data(),
@@ -253,6 +258,15 @@ public:
     use_graph_ = use;
   }
 
+  void set_serial_resample(bool serial) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    const int v = serial ? 1 : 0;
+    DUST2_CUDA(cudaMemcpy(force_serial_.data(), &v, sizeof(int),
+                          cudaMemcpyHostToDevice));
+  }
+
   filter_view view() {
     const auto& L = sys_->layout();
     (void)L;
@@ -262,7 +276,8 @@ public:
                        tile_sum_.data(), tile_off_.data(), gkey_.data(),
                        gnz_.data(), gflag_.data(), mode_.data(), ll_.data(),
                        gu_.data(), guu0_.data(), gdu_.data(), gtot_.data(),
-                       idx_.data(), frng_.data(), set_initial_.data()};
+                       idx_.data(), frng_.data(), set_initial_.data(),
+                       force_serial_.data()};
   }
 
   void run(const double* initial, const int* index_group, int n_index_group,
@@ -307,6 +322,9 @@ public:
       }
       timing_ = enable;
       graph_state_ptr_ = nullptr;  // force a re-capture
+      if (timing_) {
+        ensure_events();  // no allocation may happen during capture
+      }
     }
     step_ms_ = 0;
     run_ms_ = 0;
@@ -500,9 +518,6 @@ private:
     const int G = L.n_groups;
     const int NT = L.n_tiles();
     const int TS = L.tile_size;
-    if (fallback_count_.size() != static_cast<std::size_t>(G)) {
-      fallback_count_.resize(G);
-    }
     filter_view f = view();
     f.gflag = gflag_.data();
     if (timing_) {
@@ -645,6 +660,7 @@ private:
   device_array<std::uint64_t> frng_;
   device_array<int> set_initial_;
   device_array<int> fallback_count_;
+  device_array<int> force_serial_;
   device_array<data_type> data_;
 
   cudaGraph_t graph_ = nullptr;
@@ -658,7 +674,7 @@ __global__ void k_fallback_count(filter_view f, int* count);
 template <typename T>
 void filter_engine<T>::k_fallback_counted(filter_view f, cudaStream_t s) {
   const int G = sys_->layout().n_groups;
-  k_fallback_count<<<G, 32, 0, s>>>(f, fallback_count_.data());
+  k_fallback_count<<<G, 256, 0, s>>>(f, fallback_count_.data());
 }
 
 }  // namespace engine

@@ -113,7 +113,7 @@ __global__ void k_group(filter_view f, int n_groups) {
     f.mode[g] = mode;
     f.gkey[g] = ordered_key(-INFINITY);
     f.gnz[g] = 0;
-    f.gflag[g] = 0;
+    f.gflag[g] = (mode == MODE_RESAMPLE && *f.force_serial) ? 1 : 0;
   }
 }
 
@@ -180,13 +180,26 @@ __global__ void k_resample(filter_view f) {
   // is below or inside the first weight) and its prefix of m + 1 weights
   // reaches it (needed only for m < n - 1: the loop stops at the last
   // particle anyway).
-  const double margin = (4.0 * n + 128.0) * 0x1.0p-53 * tot;
+  //
+  // Bound, with u = 2^-53 and L = log2(n) + 2: a serial prefix of k
+  // weights differs from the exact sum S_k by at most (k - 1) u S_k; the
+  // block scan here by at most L u S_k; each weight may differ from the
+  // other side's exp by 2 ulp (4 u S_k); the target computed from either
+  // total differs by at most (n + L + 10) u uu.  So a decision is safe
+  // when the prefix is farther than (k + n + 2L + 16) u max(S_k, uu)
+  // from the target (5% slack on top).
+  const double L = 2.0 + ceil(log2(static_cast<double>(n)));
+  const double eps = 0x1.0p-53 * 1.05;
   bool ok = true;
   if (m > 0) {
-    ok = ok && prefix_at(f, g, m - 1, ts) < uu - margin;
+    const double p = prefix_at(f, g, m - 1, ts);
+    const double margin = eps * (m + n + 2 * L + 16) * fmax(p, uu);
+    ok = ok && p < uu - margin;
   }
   if (m < n - 1) {
-    ok = ok && prefix_at(f, g, m, ts) >= uu + margin;
+    const double q = prefix_at(f, g, m, ts);
+    const double margin = eps * (m + 1 + n + 2 * L + 16) * fmax(q, uu);
+    ok = ok && q >= uu + margin;
   }
   f.idx[k] = m;
   if (!ok) {
@@ -194,36 +207,70 @@ __global__ void k_resample(filter_view f) {
   }
 }
 
-// The reference algorithm verbatim (filter_details.hpp:45-74) for groups
-// with an ambiguous parallel decision.
+// The reference algorithm (filter_details.hpp:45-74) for groups with an
+// ambiguous parallel decision.  Its serial running sum ww_j =
+// fl(ww_{j-1} + w_j) is computed exactly as the reference does, by one
+// thread, with the weights staged through shared memory in chunks; the
+// reference's walk over particles then equals, for each particle, the
+// first j with ww_j >= uu_i (ww is non-decreasing because the weights are
+// non-negative and rounding is monotone), which the whole block finds by
+// binary search.  The serial sums overwrite this group's `pre` entries.
+constexpr int FALLBACK_CHUNK = 2048;
+
 __global__ void k_fallback_count(filter_view f, int* count) {
+  __shared__ double buf[FALLBACK_CHUNK];
+  __shared__ double total;
   const int g = blockIdx.x;
-  if (!f.active[g] || f.mode[g] != MODE_RESAMPLE || !f.gflag[g] ||
-      threadIdx.x != 0) {
+  if (!f.active[g] || f.mode[g] != MODE_RESAMPLE || !f.gflag[g]) {
     return;
   }
-  count[g] += 1;
   const int n = f.n_particles[g];
   const double* w = f.ew + f.offset[g];
+  double* ser = f.pre + f.offset[g];
   int* idx = f.idx + f.offset[g];
-  double tot = 0;
-  for (int j = 0; j < n; ++j) {
-    tot += w[j];
+  double run = 0;
+  for (int base = 0; base < n; base += FALLBACK_CHUNK) {
+    const int m = min(FALLBACK_CHUNK, n - base);
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      buf[i] = w[base + i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll 8
+      for (int i = 0; i < m; ++i) {
+        run = run + buf[i];
+        buf[i] = run;
+      }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      ser[base + i] = buf[i];
+    }
+    __syncthreads();
   }
+  if (threadIdx.x == 0) {
+    total = run;
+    count[g] += 1;
+    f.gflag[g] = 0;
+  }
+  __syncthreads();
+  const double tot = total;
   const double u = f.gu[g];
   const double uu0 = tot * u / n;
   const double du = tot / n;
-  double ww = 0;
-  int j = 0;
-  for (int i = 0; i < n; ++i) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double uu = uu0 + static_cast<double>(i) * du;
-    while (ww < uu && j < n) {
-      ww += w[j];
-      ++j;
+    int a = 0, b = n;  // first m with ser[m] >= uu, or n
+    while (a < b) {
+      const int mid = (a + b) >> 1;
+      if (ser[mid] >= uu) {
+        b = mid;
+      } else {
+        a = mid + 1;
+      }
     }
-    idx[i] = j == 0 ? 0 : j - 1;
+    idx[i] = a == n ? n - 1 : a;
   }
-  f.gflag[g] = 0;
 }
 
 }  // namespace engine

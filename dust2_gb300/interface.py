@@ -925,6 +925,33 @@ def dust_likelihood_last_state(obj, select_random_particle=False):
     return arr[:, :, 0]
 
 
+def resample_weight(w, u):
+    """Systematic resampling indices (0-based) of weights w with uniform u,
+    on the GPU (dust2's test_resample_weight, src/test.cpp)."""
+    w = as_f64(w)
+    idx = np.empty(w.size, dtype=np.uintp)
+    check(_lib.lib().dust2_gb300_resample_weight(dptr(w), w.size, float(u),
+                                                 sptr(idx)))
+    return idx.astype(np.int64)
+
+
+def scale_log_weights(w):
+    """(log mean weight, scaled weights) on the GPU (dust2's
+    test_scale_log_weights)."""
+    w = np.array(w, dtype=np.float64)
+    r = ctypes.c_double()
+    check(_lib.lib().dust2_gb300_scale_log_weights(dptr(w), w.size,
+                                                   ctypes.byref(r)))
+    return r.value, w
+
+
+def dust_likelihood_set_serial_resample(obj, serial):
+    """Verification mode: resample every group with the serial algorithm."""
+    _check_lik(obj)
+    check(_lib.lib().dust2_gb300_filter_set_serial_resample(
+        obj.ptr, 1 if serial else 0))
+
+
 def dust_likelihood_serial_fallbacks(obj):
     """Number of group resamplings recomputed serially (diagnostic)."""
     _check_lik(obj)

@@ -255,6 +255,29 @@ int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
 int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,
                                         int64_t* n);
 
+/* ---- filter helpers (src/test.cpp:10-23) ------------------------------- */
+
+/* test_resample_weight (filter_details.hpp:45-74): systematic resampling
+ * of n non-negative weights w with uniform u; idx receives the 0-based
+ * source particle of each of the n new particles.  Runs the filter's GPU
+ * resampling kernels (exact: ties within rounding distance fall back to
+ * the serial algorithm). */
+int dust2_gb300_resample_weight(const double* w, size_t n, double u,
+                                size_t* idx);
+
+/* test_scale_log_weights (filter_details.hpp:11-39): replaces the n log
+ * weights in w by exp(w - max) (NaN -> weight 0), and writes
+ * log(mean(exp(w - max))) + max to result; a single weight is returned
+ * unchanged; all -Inf gives -Inf with the weights left as log weights. */
+int dust2_gb300_scale_log_weights(double* w, size_t n, double* result);
+
+/* 1: resample every group with the serial algorithm of
+ * filter_details.hpp:45-74 (verification of the parallel resampler);
+ * 0 (default): parallel search with the serial algorithm only for groups
+ * whose decision is within rounding distance of a boundary. */
+int dust2_gb300_filter_set_serial_resample(dust2_gb300_filter* filter,
+                                           int32_t serial);
+
 /* Asynchronous form of dust2_gb300_filter_run (system initial conditions,
  * current parameters): enqueues the run on the filter's CUDA stream and
  * returns; results stay on the device.  No counterpart in dust2, whose

@@ -295,3 +295,73 @@ def test_filter_errors(built):
     # a failed run does not poison the next one (reset re-initialises)
     ok = {"beta": 0.1, "gamma": 0.2, "N": 1000, "I0": 10}
     assert np.isfinite(d.dust_likelihood_run(obj, ok))
+
+
+def test_forced_serial_resampling_is_identical(port):
+    """The parallel resampler with its exactness check and the serial
+    algorithm give identical filters (and both equal the oracle)."""
+    from dust2_gb300 import interface
+    n_particles = [30000, 4096, 700]
+    gen = d.sir_cases()
+    plist, times, data = _uneven_case(21, n_particles, n_times=20)
+    G = len(n_particles)
+    cols = {"time": np.repeat(times, G), "group": np.tile(np.arange(1, G + 1),
+                                                          times.size),
+            "incidence": data.ravel()}
+    res = []
+    for serial in (False, True):
+        obj = d.dust_filter_create(gen, 0, cols, n_particles=n_particles,
+                                   dt=0.25, seed=3)
+        d.dust_likelihood_run(obj, plist)
+        interface.dust_likelihood_set_serial_resample(obj, serial)
+        ll = d.dust_likelihood_run(obj, plist)
+        res.append((ll, d.dust_likelihood_last_state(obj),
+                    d.dust_likelihood_rng_state(obj)))
+        if serial:
+            assert d.dust_likelihood_serial_fallbacks(obj) >= 20 * G
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    assert res[0][2] == res[1][2]
+    assert_ll(res[0][0], res[1][0])
+
+
+def test_resample_weight_hook(port):
+    """test-filter-details.R:1-22 through the GPU kernels, including exact
+    ties, where the parallel decision must defer to the serial one."""
+    g = golden("filter_details")
+    for u, idx in zip(g["u"], g["idx"]):
+        np.testing.assert_array_equal(d.resample_weight(g["w"], u), idx)
+    rs = np.random.default_rng(5)
+    for n in (1, 2, 255, 256, 257, 5000, 100000):
+        w = np.abs(rs.standard_cauchy(n))
+        for u in (0.0, rs.uniform(), 1 - 1e-12):
+            np.testing.assert_array_equal(d.resample_weight(w, u),
+                                          port.resample_weight(w, u))
+    # every boundary an exact tie: prefix sums and targets are integers
+    w = np.ones(1000)
+    for u in (0.0, 0.5):
+        np.testing.assert_array_equal(d.resample_weight(w, u),
+                                      port.resample_weight(w, u))
+    w = np.zeros(50)
+    w[7] = 3.0
+    np.testing.assert_array_equal(d.resample_weight(w, 0.3),
+                                  port.resample_weight(w, 0.3))
+
+
+def test_scale_log_weights_hook(port):
+    """test-filter-details.R:55-64 through the GPU kernels."""
+    g = golden("filter_details")
+    r, w = d.scale_log_weights(g["lw"])
+    assert abs(r - g["lw_ret"][0]) <= 1e-12 * abs(g["lw_ret"][0])
+    np.testing.assert_allclose(w, g["lw_w1"], rtol=4.5e-16, atol=0)
+    assert w[3] == 0 and w[17] == 0
+    r, w = d.scale_log_weights(np.full(5, -np.inf))
+    assert r == -np.inf
+    np.testing.assert_array_equal(w, np.full(5, -np.inf))
+    r, w = d.scale_log_weights(np.array([-3.5]))
+    assert r == -3.5
+    rs = np.random.default_rng(8)
+    x = rs.normal(-50, 20, 70000)
+    r, w = d.scale_log_weights(x)
+    rp, wp = port.scale_log_weights(x)
+    assert abs(r - rp) <= 1e-12 * abs(rp)
+    np.testing.assert_allclose(w, wp, rtol=4.5e-16, atol=1e-300)

@@ -133,7 +133,8 @@ def test_many_instances_match_oracle(port):
     res = d.dust_system_simulate(sys, times)
     out, stats = port.ode_simulate("sirode", flat, n, 1, 0.0, times, 5,
                                    n_threads=port.max_threads())
-    got = res.transpose(3, 2, 1, 0).ravel()
+    # ungrouped-particle layout: (state, group, time)
+    got = res.reshape(5, n, times.size).transpose(2, 1, 0).ravel()
     np.testing.assert_allclose(got, out, rtol=1e-6, atol=1e-6)
     internals = d.dust_system_internals(sys)
     frac_same = np.mean(internals["n_steps"] == stats[:, 0])
