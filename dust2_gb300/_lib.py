@@ -116,6 +116,8 @@ _SIGNATURES = {
         ctypes.c_void_p, c_i64_p]),
     "dust2_gb300_resample_weight": (ctypes.c_int, [
         c_double_p, ctypes.c_size_t, ctypes.c_double, c_size_p]),
+    "dust2_gb300_resample_weight_noalloc": (ctypes.c_int, [
+        c_double_p, ctypes.c_size_t, ctypes.c_double, c_size_p]),
     "dust2_gb300_scale_log_weights": (ctypes.c_int, [
         c_double_p, ctypes.c_size_t, c_double_p]),
     "dust2_gb300_filter_set_serial_resample": (ctypes.c_int, [

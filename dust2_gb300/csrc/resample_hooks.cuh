@@ -27,6 +27,12 @@ void hook_layout(char* base, std::size_t n, int tile_size,
                  const std::vector<tile>& tiles, hook_buffers& hb,
                  cudaStream_t s);
 
+// As hook_layout, with the tiles given as a plain array (no container),
+// for the entry point that must not allocate.
+void hook_layout_fixed(char* base, std::size_t n, int tile_size,
+                       const tile* tiles, int n_tiles, hook_buffers& hb,
+                       cudaStream_t s);
+
 // Systematic resampling of the raw weights in hb.f.w with uniform u;
 // indices (group-local) are left in hb.f.idx.
 void hook_resample(hook_buffers& hb, double u, int tile_size, int serial,

@@ -271,6 +271,19 @@ int dust2_gb300_resample_weight(const double* w, size_t n, double u,
  * unchanged; all -Inf gives -Inf with the weights left as log weights. */
 int dust2_gb300_scale_log_weights(double* w, size_t n, double* result);
 
+/* dust2_gb300_resample_weight without any device allocation: the
+ * working arrays live in a fixed scratch area compiled into the library
+ * (about 1.9 MB, held by every device that loads it).  For callers that
+ * cannot allocate device memory at call time, e.g. when another allocator
+ * owns the GPU's memory or when cudaFree's device-wide synchronisation is
+ * unacceptable.  At most 65536 weights (an error otherwise).  The first
+ * call on a device looks up the scratch area's address with that device
+ * current: make it before any stream capture.  All calls share the area,
+ * so calls that overlap on the GPU race: serialise them.  No counterpart
+ * in dust2. */
+int dust2_gb300_resample_weight_noalloc(const double* w, size_t n, double u,
+                                        size_t* idx);
+
 /* 1: resample every group with the serial algorithm of
  * filter_details.hpp:45-74 (verification of the parallel resampler);
  * 0 (default): parallel search with the serial algorithm only for groups
