@@ -43,45 +43,54 @@ constexpr int MAX_REJECTION_ATTEMPTS = 100000;
 // BINV restarts when the search passes this count (the published cap).
 constexpr double BINV_MAX_X = 110;
 
+// The recurrence f(x) = f(x-1) ((n+1) s / x - s), s = p/q, uses 1/x from
+// a table, and s from a reciprocal, so the loop has no FP64 division.
 DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
   const double q = 1.0 - p;
-  const double s = p / q;
+  const double s = p * math::rcp(q);
   const double a = (n + 1.0) * s;
   const double r0 = math::exp(n * math::log(q));  // q^n
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
     double r = r0;
     double u = random_real(rng);
-    double x = 0;
+    int x = 0;
     while (u > r) {
       u = u - r;
-      x = x + 1.0;
-      r = r * (a / x - s);
+      x = x + 1;
+      r = r * (a * math::recip_int(x) - s);
       if (x > BINV_MAX_X) {
         break;
       }
     }
     if (x <= BINV_MAX_X) {
-      return x;
+      return static_cast<double>(x);
     }
   }
   set_error(rng, ERR_BINOMIAL_INVALID, n, p);
   return math::quiet_nan();
 }
 
+// Divisions by b, us, q and the hat denominator are multiplications by
+// reciprocals (math::rcp); us = 0 (u = -1/2 exactly) is rejected.
 DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
   const double q = 1.0 - p;
   const double spq = std::sqrt(n * p * q);
   const double b = 1.15 + 2.53 * spq;
   const double a = -0.0873 + 0.0248 * b + 0.01 * p;
   const double c = n * p + 0.5;
-  const double v_r = 0.92 - 4.2 / b;
+  const double inv_b = math::rcp(b);
+  const double v_r = 0.92 - 4.2 * inv_b;
   bool have_setup = false;
   double alpha = 0, lpq = 0, m = 0, h = 0;
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
     const double u = random_real(rng) - 0.5;
     double v = random_real(rng);
     const double us = 0.5 - std::fabs(u);
-    const double k = std::floor((2.0 * a / us + b) * u + c);
+    if (us == 0) {
+      continue;
+    }
+    const double inv_us = math::rcp(us);
+    const double k = std::floor((2.0 * a * inv_us + b) * u + c);
     if (us >= 0.07 && v <= v_r) {
       return k;
     }
@@ -89,13 +98,13 @@ DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
       continue;
     }
     if (!have_setup) {
-      alpha = (2.83 + 5.1 / b) * spq;
-      lpq = math::log(p / q);
+      alpha = (2.83 + 5.1 * inv_b) * spq;
+      lpq = math::log(p * math::rcp(q));
       m = std::floor((n + 1.0) * p);
       h = math::log_factorial(m) + math::log_factorial(n - m);
       have_setup = true;
     }
-    v = math::log(v * alpha / (a / (us * us) + b));
+    v = math::log(v * alpha * math::rcp(a * inv_us * inv_us + b));
     if (v <= h - math::log_factorial(k) - math::log_factorial(n - k) +
         (k - m) * lpq) {
       return k;
@@ -144,14 +153,18 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   const double slam = std::sqrt(lambda);
   const double b = 0.931 + 2.53 * slam;
   const double a = -0.059 + 0.02483 * b;
-  const double vr = 0.9277 - 3.6224 / (b - 2.0);
+  const double vr = 0.9277 - 3.6224 * math::rcp(b - 2.0);
   bool have_setup = false;
   double log_invalpha = 0, loglam = 0;
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
     const double u = random_real(rng) - 0.5;
     const double v = random_real(rng);
     const double us = 0.5 - std::fabs(u);
-    const double k = std::floor((2.0 * a / us + b) * u + lambda + 0.43);
+    if (us == 0) {
+      continue;
+    }
+    const double inv_us = math::rcp(us);
+    const double k = std::floor((2.0 * a * inv_us + b) * u + lambda + 0.43);
     if (us >= 0.07 && v <= vr) {
       return k;
     }
@@ -159,11 +172,11 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
       continue;
     }
     if (!have_setup) {
-      log_invalpha = math::log(1.1239 + 1.1328 / (b - 3.4));
+      log_invalpha = math::log(1.1239 + 1.1328 * math::rcp(b - 3.4));
       loglam = math::log(lambda);
       have_setup = true;
     }
-    if (math::log(v) + log_invalpha - math::log(a / (us * us) + b) <=
+    if (math::log(v) + log_invalpha - math::log(a * inv_us * inv_us + b) <=
         -lambda + k * loglam - math::log_factorial(k)) {
       return k;
     }

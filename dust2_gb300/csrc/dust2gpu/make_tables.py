@@ -1,0 +1,101 @@
+"""Generate dust2gpu/tables.hpp: correctly rounded constant tables for the
+table-driven exp and log of math.hpp and the reciprocals of small
+integers used by the binomial inversion sampler.
+
+Every value is computed in 60-digit decimal arithmetic and rounded once to
+the nearest double; a "lo" entry holds the rounded remainder of the exact
+value after its "hi" entry.
+
+Run:  python dust2_gb300/csrc/dust2gpu/make_tables.py
+"""
+
+from decimal import Decimal, getcontext
+from fractions import Fraction
+from pathlib import Path
+
+getcontext().prec = 60
+LN2 = Decimal(2).ln()
+
+
+def rn(x):
+    """Round a Decimal/Fraction to the nearest double."""
+    if isinstance(x, Decimal):
+        x = Fraction(x)
+    return float(x)
+
+
+def hi_lo(x):
+    hi = rn(x)
+    lo = rn(Decimal(x) - Decimal(hi))
+    return hi, lo
+
+
+def fmt(v):
+    return float(v).hex()
+
+
+def main():
+    out = []
+    out.append("// Generated by make_tables.py -- do not edit.")
+    out.append("#pragma once")
+    out.append("")
+    # exp: 2^(j/128), j = 0..127
+    out.append("// 2^(j/128) = EXP2_HI[j] + EXP2_LO[j]")
+    his, los = [], []
+    for j in range(128):
+        v = (LN2 * j / 128).exp()
+        h, lo = hi_lo(v)
+        his.append(h)
+        los.append(lo)
+    out.append("#define DUST2_EXP2_HI \\")
+    out.append(",\\\n".join("  " + ", ".join(fmt(v) for v in his[i:i + 3])
+                           for i in range(0, 128, 3)))
+    out.append("#define DUST2_EXP2_LO \\")
+    out.append(",\\\n".join("  " + ", ".join(fmt(v) for v in los[i:i + 3])
+                           for i in range(0, 128, 3)))
+    # log: F = j/256 for j = 181..363 (m in [sqrt(2)/2, sqrt(2)))
+    out.append("")
+    out.append("// For F = j/256, j = LOG_J0 + i: 1/F (rounded) and")
+    out.append("// log(F) = LOG_HI[i] + LOG_LO[i]")
+    j0, j1 = 181, 363
+    out.append(f"#define DUST2_LOG_J0 {j0}")
+    out.append(f"#define DUST2_LOG_N {j1 - j0 + 1}")
+    inv, lhi, llo = [], [], []
+    for j in range(j0, j1 + 1):
+        F = Fraction(j, 256)
+        inv.append(rn(1 / F))
+        v = (Decimal(j) / Decimal(256)).ln()
+        h, lo = hi_lo(v)
+        lhi.append(h)
+        llo.append(lo)
+    for name, vals in (("DUST2_LOG_INV", inv), ("DUST2_LOG_HI", lhi),
+                       ("DUST2_LOG_LO", llo)):
+        out.append(f"#define {name} \\")
+        out.append(",\\\n".join(
+            "  " + ", ".join(fmt(v) for v in vals[i:i + 3])
+            for i in range(0, len(vals), 3)))
+    # 1/x for x = 0..128 (entry 0 unused)
+    out.append("")
+    out.append("// 1/x, x = 0..128 (entry 0 is 0)")
+    rec = [0.0] + [rn(Fraction(1, x)) for x in range(1, 129)]
+    out.append("#define DUST2_RECIP_INT \\")
+    out.append(",\\\n".join("  " + ", ".join(fmt(v) for v in rec[i:i + 3])
+                           for i in range(0, len(rec), 3)))
+    # constants
+    out.append("")
+    h, lo = hi_lo(LN2 / 128)
+    # split ln2/128 so that k * hi is exact for |k| < 2^18
+    hi_bits = rn(Fraction(LN2 / 128).limit_denominator(1 << 60))
+    import math
+    m, e = math.frexp(h)
+    hi35 = math.ldexp(math.floor(math.ldexp(m, 35)), e - 35)
+    lo35 = rn(Decimal(LN2) / 128 - Decimal(hi35))
+    out.append(f"#define DUST2_LN2_128_HI {fmt(hi35)}")
+    out.append(f"#define DUST2_LN2_128_LO {fmt(lo35)}")
+    out.append(f"#define DUST2_INV_LN2_128 {fmt(rn(128 / LN2))}")
+    del hi_bits, lo
+    Path(__file__).with_name("tables.hpp").write_text("\n".join(out) + "\n")
+
+
+if __name__ == "__main__":
+    main()

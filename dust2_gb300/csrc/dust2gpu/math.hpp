@@ -7,16 +7,19 @@
 // after the first differently-rounded draw.  Everything here is therefore
 // written from textbook methods using only correctly rounded IEEE
 // operations, so that the host oracle and the kernels produce identical
-// bits:
+// bits.  GB300 executes FP64 at 1/64 of its FP32 rate, so the methods are
+// chosen to need few FP64 operations and no FP64 division:
 //
-//   exp    Cody & Waite (1980) additive range reduction x = k ln2 + r,
-//          |r| <= ln2/2, then the Taylor series of e^r to degree 13 in
-//          Horner form (truncation < 5e-18 relative), scaled by 2^k.
-//   log    x = 2^e m with m in [sqrt(2)/2, sqrt(2)), then
-//          log(m) = 2 atanh(s), s = (m-1)/(m+1), summed as the odd series
-//          2 s^(2k+1)/(2k+1) in s^2 (11 terms), recombined in the
-//          "f - (hf^2/2 - s (hf^2/2 + R))" form that keeps the leading
-//          term exact.
+//   exp    table-driven (Tang 1989): x = (128 k + j) ln2/128 + r with a
+//          two-part ln2/128 (exact k * hi), |r| <= ln2/256, then
+//          2^(j/128) (double-double table) * (1 + expm1(r)), expm1 by its
+//          Taylor polynomial through r^5, scaled by 2^k.
+//   log    table-driven (Tang 1990): x = 2^e m, m in [sqrt(2)/2, sqrt(2)),
+//          F = j/256 nearest to m, r = (m - F) * (1/F) (m - F exact), then
+//          log(x) = e ln2 + log(F) (double-double table) + log1p(r) by its
+//          Taylor polynomial through r^7.
+//   rcp    1/y from the correctly rounded FP32 reciprocal of (float)y
+//          (cheap on this GPU) refined by two Newton steps in FP64 FMA.
 //   lgamma for x > 0: exact table of log(k!) for integer arguments below
 //          30; otherwise the argument is shifted up to >= 10 with the
 //          recurrence Gamma(x+1) = x Gamma(x) and the Stirling series
@@ -25,8 +28,8 @@
 //          quadrant reduction on the turn count (exact), then Taylor
 //          series of cos and sin on |x| <= pi/4.
 //
-// All constants below are the correctly rounded doubles of the stated
-// exact rationals or mathematical constants.
+// All constants below and in tables.hpp (make_tables.py) are the correctly
+// rounded doubles of the stated exact rationals or mathematical constants.
 #pragma once
 
 #include <cmath>
@@ -35,6 +38,7 @@
 #include <limits>
 
 #include "common.hpp"
+#include "tables.hpp"
 
 namespace dust2gpu {
 namespace math {
@@ -105,6 +109,30 @@ constexpr double HALF_LOG_2PI = 0x1.d67f1c864beb5p-1;  // log(2 pi) / 2
 constexpr double EXP_OVERFLOW = 0x1.62e42fefa39efp+9;
 constexpr double EXP_UNDERFLOW = -0x1.74910d52d3051p+9;
 
+// Paired constant tables: device code reads global memory (lanes index
+// different entries, which constant memory would serialise), host code a
+// plain array with the same values.
+#if defined(__CUDACC__)
+#define DUST2_TABLE(name, n, values)                                      \
+  __device__ const double name##_dev[n] = {values};                      \
+  inline const double name##_host[n] = {values};
+#else
+#define DUST2_TABLE(name, n, values)                                      \
+  inline const double name##_host[n] = {values};
+#endif
+#if defined(__CUDA_ARCH__)
+#define DUST2_TAB(name, i) (name##_dev[i])
+#else
+#define DUST2_TAB(name, i) (name##_host[i])
+#endif
+
+DUST2_TABLE(exp2_hi, 128, DUST2_EXP2_HI)
+DUST2_TABLE(exp2_lo, 128, DUST2_EXP2_LO)
+DUST2_TABLE(log_inv, DUST2_LOG_N, DUST2_LOG_INV)
+DUST2_TABLE(log_hi, DUST2_LOG_N, DUST2_LOG_HI)
+DUST2_TABLE(log_lo, DUST2_LOG_N, DUST2_LOG_LO)
+DUST2_TABLE(recip_int, 129, DUST2_RECIP_INT)
+
 DUST2_HD double exp(double x) {
   if (is_nan(x)) {
     return x;
@@ -115,26 +143,20 @@ DUST2_HD double exp(double x) {
   if (x < EXP_UNDERFLOW) {
     return 0.0;
   }
-  const double kf = std::rint(x * LOG2E);
+  const double kf = std::rint(x * DUST2_INV_LN2_128);
   const int k = static_cast<int>(kf);
-  double r = std::fma(-kf, LN2_HI, x);
-  r = std::fma(-kf, LN2_LO, r);
-  // Taylor coefficients 1/j!, j = 13 .. 0
-  double p = 0x1.6124613a86d09p-33;
-  p = std::fma(p, r, 0x1.1eed8eff8d898p-29);
-  p = std::fma(p, r, 0x1.ae64567f544e4p-26);
-  p = std::fma(p, r, 0x1.27e4fb7789f5cp-22);
-  p = std::fma(p, r, 0x1.71de3a556c734p-19);
-  p = std::fma(p, r, 0x1.a01a01a01a01ap-16);
-  p = std::fma(p, r, 0x1.a01a01a01a01ap-13);
-  p = std::fma(p, r, 0x1.6c16c16c16c17p-10);
-  p = std::fma(p, r, 0x1.1111111111111p-7);
-  p = std::fma(p, r, 0x1.5555555555555p-5);
+  double r = std::fma(-kf, DUST2_LN2_128_HI, x);
+  r = std::fma(-kf, DUST2_LN2_128_LO, r);
+  const int j = k & 127;
+  const int e = (k - j) / 128;
+  // expm1(r) = r + r^2 (1/2 + r (1/6 + r (1/24 + r / 120)))
+  double p = std::fma(r, 0x1.1111111111111p-7, 0x1.5555555555555p-5);
   p = std::fma(p, r, 0x1.5555555555555p-3);
-  p = std::fma(p, r, 0x1.0000000000000p-1);
-  p = std::fma(p, r, 1.0);
-  p = std::fma(p, r, 1.0);
-  return scale2(p, k);
+  p = std::fma(p, r, 0.5);
+  const double pm1 = std::fma(r * r, p, r);
+  const double t_hi = DUST2_TAB(exp2_hi, j);
+  const double t_lo = DUST2_TAB(exp2_lo, j);
+  return scale2(t_hi + std::fma(t_hi, pm1, t_lo), e);
 }
 
 DUST2_HD double log(double x) {
@@ -159,26 +181,37 @@ DUST2_HD double log(double x) {
     m = from_bits((bits_of(m) & 0x000fffffffffffffull) | 0x3fe0000000000000ull);
     e += 1;
   }
-  const double f = m - 1.0;  // exact (Sterbenz)
-  const double s = f / (2.0 + f);
-  const double z = s * s;
-  // R = sum_{k>=1} 2 z^k / (2k+1), k = 1..11
-  double R = 0x1.642c8590b2164p-4;
-  R = std::fma(R, z, 0x1.8618618618618p-4);
-  R = std::fma(R, z, 0x1.af286bca1af28p-4);
-  R = std::fma(R, z, 0x1.e1e1e1e1e1e1ep-4);
-  R = std::fma(R, z, 0x1.1111111111111p-3);
-  R = std::fma(R, z, 0x1.3b13b13b13b14p-3);
-  R = std::fma(R, z, 0x1.745d1745d1746p-3);
-  R = std::fma(R, z, 0x1.c71c71c71c71cp-3);
-  R = std::fma(R, z, 0x1.2492492492492p-2);
-  R = std::fma(R, z, 0x1.999999999999ap-2);
-  R = std::fma(R, z, 0x1.5555555555555p-1);
-  R = R * z;
-  const double hfsq = 0.5 * f * f;
-  const double logm = f - (hfsq - s * (hfsq + R));
+  const int j = static_cast<int>(std::rint(m * 256.0));
+  const double f = m - static_cast<double>(j) * 0x1p-8;  // exact
+  const int i = j - DUST2_LOG_J0;
+  const double r = f * DUST2_TAB(log_inv, i);
+  // log1p(r) = r + r^2 (-1/2 + r (1/3 + r (-1/4 + r (1/5 + r (-1/6 + r/7)))))
+  double p = std::fma(r, 0x1.2492492492492p-3, -0x1.5555555555555p-3);
+  p = std::fma(p, r, 0x1.999999999999ap-3);
+  p = std::fma(p, r, -0.25);
+  p = std::fma(p, r, 0x1.5555555555555p-2);
+  p = std::fma(p, r, -0.5);
+  const double lp = std::fma(r * r, p, r);
   const double ef = static_cast<double>(e);
-  return std::fma(ef, LN2_HI, std::fma(ef, LN2_LO, logm));
+  const double hi = std::fma(ef, LN2_HI, DUST2_TAB(log_hi, i));
+  const double lo = std::fma(ef, LN2_LO, DUST2_TAB(log_lo, i)) + lp;
+  return hi + lo;
+}
+
+// 1/y for finite y with |y| in [1e-30, 1e30] (within 1 ulp; not
+// correctly rounded).
+DUST2_HD double rcp(double y) {
+  const double r0 =
+    static_cast<double>(1.0f / static_cast<float>(y));
+  double e = std::fma(-y, r0, 1.0);
+  double r = std::fma(r0, e, r0);
+  e = std::fma(-y, r, 1.0);
+  return std::fma(r, e, r);
+}
+
+// 1/x for integer x in [1, 128] (correctly rounded, from a table).
+DUST2_HD double recip_int(int x) {
+  return DUST2_TAB(recip_int, x);
 }
 
 // log(k!) for k = 0..29, correctly rounded.  One copy per side: device
@@ -214,7 +247,7 @@ DUST2_HD double log_factorial_table(int k) {
 
 // Stirling series for log Gamma(y), y >= 10.
 DUST2_HD double lgamma_stirling(double y) {
-  const double t = 1.0 / y;
+  const double t = rcp(y);
   const double t2 = t * t;
   // B_2k / (2k (2k-1)), k = 7 .. 1
   double s = 0x1.a41a41a41a41ap-8;
