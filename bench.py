@@ -45,10 +45,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 # Executed FP64 operations (DADD + DMUL + 2 DFMA, per thread) per
-# particle-step of the step+compare kernel on this workload, from the ncu
-# SASS counters summarised in profiles/ (see the design doc).  None until
-# measured.
-FP64_OPS_PER_PARTICLE_STEP = None
+# particle-step of the step+compare kernel, per workload, from the ncu SASS
+# counters of that kernel over a whole likelihood run (summaries under
+# profiles/).  A workload without an entry reports no achieved rate.
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 273.9}
 STEPS_PER_OBS = 4  # dt = 0.25, daily observations
 
 
@@ -59,7 +59,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--workload", default="sir_batched",
-                   choices=["sir_batched", "sir_small"])
+                   choices=["sir_batched", "sir_small", "seir_batched"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU sample")
@@ -140,13 +140,23 @@ def fp64_peak_tflops():
     return t.value
 
 
+N_STATE = {"sir_cases": 4, "sir": 5, "seir_age": 96}
+
+
 def build_workload(name, simulate):
     from dust2_gb300 import workloads
     if name == "sir_batched":
-        return workloads.sir_batched(simulate)
-    w = workloads.sir_small(simulate)
-    w["data"] = w["data"].reshape(-1, 1)
-    w["n_particles"] = [w["n_particles"]]
+        w = workloads.sir_batched(simulate)
+        w["system"] = "sir_cases"
+    elif name == "seir_batched":
+        w = workloads.seir_batched(simulate)
+        w["system"] = "seir_age"
+    else:
+        w = workloads.sir_small(simulate)
+        w["data"] = w["data"].reshape(-1, 1)
+        w["n_particles"] = [w["n_particles"]]
+        w["system"] = "sir_cases"
+    w["n_state"] = N_STATE[w["system"]]
     return w
 
 
@@ -167,16 +177,16 @@ def run_cpu(w, n_groups, n_threads, n_runs=1):
     port = pyoracle.port()
     npg = w["n_particles"][:n_groups]
     G_all = len(w["n_particles"])
-    gen = d.sir_cases()
+    gen = d.Generator(w["system"])
     npar = gen.n_pars
     pars = np.asarray(w["pars"]).reshape(G_all, npar)[:n_groups].ravel()
     data = np.asarray(w["data"]).reshape(w["times"].size, G_all)[:, :n_groups]
     n_streams = sum(n + 2 for n in npg)
     rng = np.frombuffer(d.rng_streams(n_streams, w["seed"]), dtype="<u8")
     t0 = time.perf_counter()
-    port.filter_run("sir_cases", pars, npg, 0.0, w["times"], data.ravel(),
-                    n_groups, w["dt"], rng, n_runs=n_runs, n_state=4,
-                    n_threads=n_threads)
+    port.filter_run(w["system"], pars, npg, 0.0, w["times"], data.ravel(),
+                    n_groups, w["dt"], rng, n_runs=n_runs,
+                    n_state=w["n_state"], n_threads=n_threads)
     dt = (time.perf_counter() - t0) / n_runs
     ps = sum(npg) * w["times"].size * STEPS_PER_OBS
     return dt, ps
@@ -219,7 +229,7 @@ def gpu_simulate_factory():
             None, _lib.uptr(words), 1, 0, ctypes.byref(h)))
         try:
             _lib.check(_lib.lib().dust2_gb300_system_set_state_initial(h))
-            n_state = {"sir_cases": 4, "sir": 5}[name]
+            n_state = N_STATE[name]
             out = np.empty(times.size * n_groups * n_particles * n_state)
             _lib.check(_lib.lib().dust2_gb300_system_simulate(
                 h, _lib.dptr(times), times.size, None, 0, _lib.dptr(out)))
@@ -245,7 +255,7 @@ def gpu_arm(args, rank, world, local):
     from dust2_gb300 import _lib
 
     w = build_workload(args.workload, gpu_simulate_factory())
-    gen = d.sir_cases()
+    gen = d.Generator(w["system"])
     npg = w["n_particles"]
     obj = d.dust_filter_create(gen, 0, data_columns(w),
                                n_particles=npg if len(npg) > 1 else npg[0],
@@ -340,12 +350,12 @@ def gpu_arm(args, rank, world, local):
         ps_per_launch = n_total * STEPS_PER_OBS
         achieved = None
         frac = None
-        if FP64_OPS_PER_PARTICLE_STEP is not None:
-            achieved = (FP64_OPS_PER_PARTICLE_STEP * ps_per_launch /
-                        (step_launch_ms * 1e-3) / 1e12)
+        ops = FP64_OPS_PER_PARTICLE_STEP.get(args.workload)
+        if ops is not None:
+            achieved = (ops * ps_per_launch / (step_launch_ms * 1e-3) / 1e12)
             frac = achieved / peak
         roofline = {
-            "bound": "fp64", "kernel": "k_step_compare<sir_cases>",
+            "bound": "fp64", "kernel": f"k_step_compare<{w['system']}>",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": frac, "traffic": None,
             "peak_source": "measured in-process: DFMA-chain microbenchmark "
@@ -436,7 +446,7 @@ def oracle_simulate():
                             dtype="<u8")
         out, _ = pyoracle.port().discrete_simulate(
             name, flat, n_groups, n_particles, 0.0, dt, rng, times)
-        n_state = {"sir_cases": 4, "sir": 5}[name]
+        n_state = N_STATE[name]
         return out[:times.size * n_groups * n_particles * n_state]
     return simulate
 

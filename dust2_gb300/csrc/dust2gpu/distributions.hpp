@@ -41,10 +41,16 @@ namespace random {
 // acceptance rate is above 0.8, so reaching this means corrupt input.
 constexpr int MAX_REJECTION_ATTEMPTS = 100000;
 // BINV restarts when the search passes this count (the published cap).
-constexpr double BINV_MAX_X = 110;
+constexpr int BINV_MAX_X = 110;
+
+// Comparisons whose operands are known to be non-negative (uniforms,
+// probabilities, the inversion remainder) are taken on the bit patterns
+// (math::gt_nonneg / le_nonneg); they decide exactly as the FP64
+// comparison would.
 
 // The recurrence f(x) = f(x-1) ((n+1) s / x - s), s = p/q, uses 1/x from
 // a table, and s from a reciprocal, so the loop has no FP64 division.
+// u stays >= 0 (it only loses a smaller r), so `u > r` is a bit compare.
 DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
   const double q = 1.0 - p;
   const double s = p * math::rcp(q);
@@ -54,7 +60,7 @@ DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
     double r = r0;
     double u = random_real(rng);
     int x = 0;
-    while (u > r) {
+    while (math::gt_nonneg(u, r)) {
       u = u - r;
       x = x + 1;
       r = r * (a * math::recip_int(x) - s);
@@ -71,7 +77,8 @@ DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
 }
 
 // Divisions by b, us, q and the hat denominator are multiplications by
-// reciprocals (math::rcp); us = 0 (u = -1/2 exactly) is rejected.
+// reciprocals (math::rcp); us = 0 (u = -1/2 exactly) is rejected.  Here
+// n p >= 10 and q >= 1/2, so b > 6.8 and v_r > 0.3.
 DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
   const double q = 1.0 - p;
   const double spq = std::sqrt(n * p * q);
@@ -80,21 +87,25 @@ DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
   const double c = n * p + 0.5;
   const double inv_b = math::rcp(b);
   const double v_r = 0.92 - 4.2 * inv_b;
+  const std::int64_t n_bits = static_cast<std::int64_t>(math::bits_of(n));
   bool have_setup = false;
   double alpha = 0, lpq = 0, m = 0, h = 0;
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
     const double u = random_real(rng) - 0.5;
     double v = random_real(rng);
-    const double us = 0.5 - std::fabs(u);
-    if (us == 0) {
+    const double us = 0.5 - math::abs_bits(u);  // >= +0
+    if (math::bits_of(us) == 0) {
       continue;
     }
     const double inv_us = math::rcp(us);
     const double k = std::floor((2.0 * a * inv_us + b) * u + c);
-    if (us >= 0.07 && v <= v_r) {
+    if (math::le_nonneg(0.07, us) && math::le_nonneg(v, v_r)) {
       return k;
     }
-    if (k < 0 || k > n) {
+    // k < 0 || k > n (k is never -0: the floored sum is >= -0.5 + c > 0
+    // or an exact negative integer)
+    const std::int64_t k_bits = static_cast<std::int64_t>(math::bits_of(k));
+    if (k_bits < 0 || k_bits > n_bits) {
       continue;
     }
     if (!have_setup) {
@@ -114,34 +125,43 @@ DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
   return math::quiet_nan();
 }
 
-// Binomial(n, p) for integer-valued n >= 0 and p in [0, 1].
+// Binomial(n, p) for integer-valued n >= 0 and p in [0, 1].  The argument
+// checks are taken on the bit patterns, with the FP64 semantics of
+// !(n >= 0) || !finite(n) || !(p >= 0) || !(p <= 1) (so -0 is valid).
 DUST2_HD double binomial(rng_state& rng, double n, double p) {
-  if (!(n >= 0) || !math::is_finite(n) || !(p >= 0) || !(p <= 1)) {
+  const std::uint64_t nb = math::bits_of(n);
+  const std::uint64_t pb = math::bits_of(p);
+  constexpr std::uint64_t MINUS_ZERO = 0x8000000000000000ull;
+  const bool n_ok = nb < 0x7ff0000000000000ull || nb == MINUS_ZERO;
+  const bool p_ok = pb <= 0x3ff0000000000000ull || pb == MINUS_ZERO;
+  if (!n_ok || !p_ok) {
     set_error(rng, ERR_BINOMIAL_INVALID, n, p);
     return math::quiet_nan();
   }
   if (rng.deterministic) {
     return n * p;
   }
-  if (n == 0 || p == 0) {
+  if ((nb << 1) == 0 || (pb << 1) == 0) {  // n == 0 || p == 0
     return 0;
   }
-  if (p == 1) {
+  if (pb == 0x3ff0000000000000ull) {  // p == 1
     return n;
   }
-  const bool flip = p > 0.5;
+  const bool flip = pb > 0x3fe0000000000000ull;  // p > 1/2
   const double pp = flip ? 1.0 - p : p;
-  const double x = (n * pp < 10) ? binomial_inversion(rng, n, pp) :
+  // n * pp < 10 (n * pp is positive and finite)
+  const bool small_mean = math::bits_of(n * pp) < 0x4024000000000000ull;
+  const double x = small_mean ? binomial_inversion(rng, n, pp) :
     binomial_btrs(rng, n, pp);
   return flip ? n - x : x;
 }
 
 DUST2_HD double poisson_knuth(rng_state& rng, double lambda) {
-  const double enlam = math::exp(-lambda);
+  const double enlam = math::exp(-lambda);  // > 0 for lambda < 10
   double prod = 1.0;
   for (int x = 0; x < MAX_REJECTION_ATTEMPTS; ++x) {
     prod = prod * random_real(rng);
-    if (prod <= enlam) {
+    if (math::le_nonneg(prod, enlam)) {
       return x;
     }
   }
@@ -149,6 +169,7 @@ DUST2_HD double poisson_knuth(rng_state& rng, double lambda) {
   return math::quiet_nan();
 }
 
+// lambda >= 10, so b > 8.9 and vr > 0.4.
 DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   const double slam = std::sqrt(lambda);
   const double b = 0.931 + 2.53 * slam;
@@ -159,16 +180,18 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
     const double u = random_real(rng) - 0.5;
     const double v = random_real(rng);
-    const double us = 0.5 - std::fabs(u);
-    if (us == 0) {
+    const double us = 0.5 - math::abs_bits(u);  // >= +0
+    if (math::bits_of(us) == 0) {
       continue;
     }
     const double inv_us = math::rcp(us);
     const double k = std::floor((2.0 * a * inv_us + b) * u + lambda + 0.43);
-    if (us >= 0.07 && v <= vr) {
+    if (math::le_nonneg(0.07, us) && math::le_nonneg(v, vr)) {
       return k;
     }
-    if (k < 0 || (us < 0.013 && v > us)) {
+    // k < 0 || (us < 0.013 && v > us); k is never -0
+    if (static_cast<std::int64_t>(math::bits_of(k)) < 0 ||
+        (!math::le_nonneg(0.013, us) && !math::le_nonneg(v, us))) {
       continue;
     }
     if (!have_setup) {
@@ -185,18 +208,22 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   return math::quiet_nan();
 }
 
+// Poisson(lambda) for lambda >= 0 (checks on the bits, with the FP64
+// semantics of !(lambda >= 0) || !finite(lambda)).
 DUST2_HD double poisson(rng_state& rng, double lambda) {
-  if (!(lambda >= 0) || !math::is_finite(lambda)) {
+  const std::uint64_t lb = math::bits_of(lambda);
+  if (!(lb < 0x7ff0000000000000ull || lb == 0x8000000000000000ull)) {
     set_error(rng, ERR_POISSON_INVALID, lambda, 0);
     return math::quiet_nan();
   }
   if (rng.deterministic) {
     return lambda;
   }
-  if (lambda == 0) {
+  if ((lb << 1) == 0) {
     return 0;
   }
-  return lambda < 10 ? poisson_knuth(rng, lambda) : poisson_ptrs(rng, lambda);
+  return lb < 0x4024000000000000ull ? poisson_knuth(rng, lambda) :
+    poisson_ptrs(rng, lambda);
 }
 
 DUST2_HD double exponential_rate(rng_state& rng, double rate) {

@@ -23,10 +23,17 @@
 //   lgamma for x > 0: exact table of log(k!) for integer arguments below
 //          30; otherwise the argument is shifted up to >= 10 with the
 //          recurrence Gamma(x+1) = x Gamma(x) and the Stirling series
-//          with Bernoulli coefficients B_2k / (2k (2k-1)), k = 1..7.
+//          with Bernoulli coefficients B_2k / (2k (2k-1)), k = 1..7.  On
+//          the device, integer arguments up to 2^20 + 1 are read from a
+//          table that the device filled with these same values.
 //   cos_2pi / sin_2pi (argument in turns) for the Box-Muller transform:
 //          quadrant reduction on the turn count (exact), then Taylor
 //          series of cos and sin on |x| <= pi/4.
+//
+// Range checks, rounding to an integer, scaling by powers of two and the
+// FP64 <-> FP32 conversions are done on the bit patterns where that is
+// exact: every FP64 instruction, comparisons and conversions included,
+// occupies the one slow FP64 pipe of this GPU.
 //
 // All constants below and in tables.hpp (make_tables.py) are the correctly
 // rounded doubles of the stated exact rationals or mathematical constants.
@@ -133,7 +140,52 @@ DUST2_TABLE(log_hi, DUST2_LOG_N, DUST2_LOG_HI)
 DUST2_TABLE(log_lo, DUST2_LOG_N, DUST2_LOG_LO)
 DUST2_TABLE(recip_int, 129, DUST2_RECIP_INT)
 
-DUST2_HD double exp(double x) {
+// Integer-pipe helpers.  On this GPU every FP64 instruction (arithmetic,
+// comparison, rounding, conversion) shares one slow pipe, so decisions
+// that can be taken on the bit patterns are taken there, exactly.
+
+// a > b for doubles a >= +0 and b not NaN (b may be negative or -0; a
+// and b must not both be zeros of different sign with a = +0, b = -0).
+DUST2_HD bool gt_nonneg(double a, double b) {
+  return static_cast<std::int64_t>(bits_of(a)) >
+    static_cast<std::int64_t>(bits_of(b));
+}
+
+// a <= b for doubles a, b >= +0 (neither NaN nor -0).
+DUST2_HD bool le_nonneg(double a, double b) {
+  return bits_of(a) <= bits_of(b);
+}
+
+// |x| by clearing the sign bit.
+DUST2_HD double abs_bits(double x) {
+  return from_bits(bits_of(x) & 0x7fffffffffffffffull);
+}
+
+// m * 2^-53 for an integer 0 <= m < 2^53, assembled from its bits (the
+// value is exact, the same as static_cast<double>(m) * 2^-53).
+DUST2_HD double u53_to_unit(std::uint64_t m) {
+  if (m == 0) {
+    return 0.0;
+  }
+#if defined(__CUDA_ARCH__)
+  const int lz = __clzll(static_cast<long long>(m)) - 11;
+#else
+  const int lz = __builtin_clzll(m) - 11;
+#endif
+  // m has 53 - lz significant bits; the leading one moves to bit 52
+  const std::uint64_t mant = (m << lz) & 0x000fffffffffffffull;
+  const std::uint64_t expo = static_cast<std::uint64_t>(1023 - 1 - lz);
+  return from_bits((expo << 52) | mant);
+}
+
+// |x| below this (704) takes the fast path of exp: the result is normal
+// and the scaling by 2^e is an exponent add.
+constexpr std::uint64_t EXP_FAST_BITS = 0x4086000000000000ull;
+// 1.5 * 2^52: adding it to |v| < 2^51 rounds v to an integer (ties to
+// even, the same as rint) in the low mantissa bits.
+constexpr double ROUND_SHIFTER = 0x1.8p52;
+
+DUST2_HD double exp_slow(double x) {
   if (is_nan(x)) {
     return x;
   }
@@ -149,7 +201,6 @@ DUST2_HD double exp(double x) {
   r = std::fma(-kf, DUST2_LN2_128_LO, r);
   const int j = k & 127;
   const int e = (k - j) / 128;
-  // expm1(r) = r + r^2 (1/2 + r (1/6 + r (1/24 + r / 120)))
   double p = std::fma(r, 0x1.1111111111111p-7, 0x1.5555555555555p-5);
   p = std::fma(p, r, 0x1.5555555555555p-3);
   p = std::fma(p, r, 0.5);
@@ -159,30 +210,72 @@ DUST2_HD double exp(double x) {
   return scale2(t_hi + std::fma(t_hi, pm1, t_lo), e);
 }
 
+DUST2_HD double exp(double x) {
+  if ((bits_of(x) & 0x7fffffffffffffffull) >= EXP_FAST_BITS) {
+    return exp_slow(x);  // NaN, infinities, |x| >= 704
+  }
+  // k = rint(x * 128/ln2), |k| < 2^17, read from the shifted sum's bits
+  const double shifted = x * DUST2_INV_LN2_128 + ROUND_SHIFTER;
+  const double kf = shifted - ROUND_SHIFTER;
+  const int k = static_cast<int>(static_cast<std::uint32_t>(bits_of(shifted)));
+  double r = std::fma(-kf, DUST2_LN2_128_HI, x);
+  r = std::fma(-kf, DUST2_LN2_128_LO, r);
+  const int j = k & 127;
+  const int e = k >> 7;  // (k - j) / 128, exact
+  // expm1(r) = r + r^2 (1/2 + r (1/6 + r (1/24 + r / 120)))
+  double p = std::fma(r, 0x1.1111111111111p-7, 0x1.5555555555555p-5);
+  p = std::fma(p, r, 0x1.5555555555555p-3);
+  p = std::fma(p, r, 0.5);
+  const double pm1 = std::fma(r * r, p, r);
+  const double t_hi = DUST2_TAB(exp2_hi, j);
+  const double t_lo = DUST2_TAB(exp2_lo, j);
+  // v in [2^(-1/256), 2); v * 2^e is normal for |e| <= 1016, so the
+  // product is the exponent add below
+  const double v = t_hi + std::fma(t_hi, pm1, t_lo);
+  return from_bits(bits_of(v) + (static_cast<std::uint64_t>(
+                                   static_cast<std::int64_t>(e)) << 52));
+}
+
 DUST2_HD double log(double x) {
-  if (is_nan(x) || x < 0) {
-    return quiet_nan();
-  }
-  if (x == 0) {
-    return -infinity();
-  }
-  if (!is_finite(x)) {
-    return x;
-  }
   std::uint64_t u = bits_of(x);
-  int e = static_cast<int>(u >> 52) - 1023;
-  if (e == -1023) {
+  int e_adj = 0;
+  // positive normal finite numbers have u in [2^52, 0x7ff0...)
+  if (u - 0x0010000000000000ull >= 0x7fe0000000000000ull) {
+    if (is_nan(x) || x < 0) {
+      return quiet_nan();
+    }
+    if (x == 0) {
+      return -infinity();
+    }
+    if (!is_finite(x)) {
+      return x;
+    }
     // subnormal: renormalise exactly
     u = bits_of(x * 0x1p54);
-    e = static_cast<int>(u >> 52) - 1023 - 54;
+    e_adj = -54;
   }
-  double m = from_bits((u & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
-  if (m > SQRT2) {
-    m = from_bits((bits_of(m) & 0x000fffffffffffffull) | 0x3fe0000000000000ull);
+  const std::uint64_t mant = u & 0x000fffffffffffffull;
+  int e = static_cast<int>(u >> 52) - 1023 + e_adj;
+  // m = 1.mant; if m > sqrt(2) use m / 2 (compare the mantissa bits)
+  const bool half = mant > (0x3ff6a09e667f3bcdull & 0x000fffffffffffffull);
+  // j = rint(256 m) from the mantissa bits (ties to even), and j / 256
+  // assembled as a double; m - j/256 is then exact
+  const int s = half ? 45 : 44;
+  const std::uint64_t q =
+    (mant + (1ull << (s - 1)) - 1 + ((mant >> s) & 1)) >> s;
+  int j;
+  double m, jd;
+  if (half) {
     e += 1;
+    j = 128 + static_cast<int>(q);
+    m = from_bits(mant | 0x3fe0000000000000ull);
+    jd = from_bits(0x3fe0000000000000ull + (q << 45));
+  } else {
+    j = 256 + static_cast<int>(q);
+    m = from_bits(mant | 0x3ff0000000000000ull);
+    jd = from_bits(0x3ff0000000000000ull + (q << 44));
   }
-  const int j = static_cast<int>(std::rint(m * 256.0));
-  const double f = m - static_cast<double>(j) * 0x1p-8;  // exact
+  const double f = m - jd;  // exact
   const int i = j - DUST2_LOG_J0;
   const double r = f * DUST2_TAB(log_inv, i);
   // log1p(r) = r + r^2 (-1/2 + r (1/3 + r (-1/4 + r (1/5 + r (-1/6 + r/7)))))
@@ -198,11 +291,53 @@ DUST2_HD double log(double x) {
   return hi + lo;
 }
 
+DUST2_HD float float_from_bits(std::uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float x;
+  std::memcpy(&x, &u, sizeof(x));
+  return x;
+#endif
+}
+
+DUST2_HD std::uint32_t float_bits_of(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  std::uint32_t u;
+  std::memcpy(&u, &x, sizeof(u));
+  return u;
+#endif
+}
+
 // 1/y for finite y with |y| in [1e-30, 1e30] (within 1 ulp; not
-// correctly rounded).
+// correctly rounded).  The seed is the correctly rounded FP32 reciprocal
+// of (float)y; both conversions between FP64 and FP32 are done on the
+// bits (round to nearest even, as the conversion instruction would).
 DUST2_HD double rcp(double y) {
-  const double r0 =
-    static_cast<double>(1.0f / static_cast<float>(y));
+  const std::uint64_t u = bits_of(y);
+  const std::uint64_t fe = ((u >> 52) & 0x7ff) - 1023 + 127;
+  if (fe - 1 >= 252) {
+    // (float)y or its reciprocal is not a normal float (or y is 0, inf,
+    // NaN): convert with the instructions
+    const double r0 = static_cast<double>(1.0f / static_cast<float>(y));
+    double e = std::fma(-y, r0, 1.0);
+    double r = std::fma(r0, e, r0);
+    e = std::fma(-y, r, 1.0);
+    return std::fma(r, e, r);
+  }
+  std::uint32_t t = static_cast<std::uint32_t>(
+    (fe << 23) | ((u >> 29) & 0x7fffffu));
+  const std::uint32_t rem = static_cast<std::uint32_t>(u & 0x1fffffffu);
+  t += (rem > 0x10000000u || (rem == 0x10000000u && (t & 1))) ? 1 : 0;
+  const float yf =
+    float_from_bits(t | static_cast<std::uint32_t>((u >> 32) & 0x80000000u));
+  const std::uint32_t rb = float_bits_of(1.0f / yf);
+  const double r0 = from_bits(
+    (static_cast<std::uint64_t>(rb & 0x80000000u) << 32) |
+    ((static_cast<std::uint64_t>((rb >> 23) & 0xff) - 127 + 1023) << 52) |
+    (static_cast<std::uint64_t>(rb & 0x7fffffu) << 29));
   double e = std::fma(-y, r0, 1.0);
   double r = std::fma(r0, e, r0);
   e = std::fma(-y, r, 1.0);
@@ -261,8 +396,9 @@ DUST2_HD double lgamma_stirling(double y) {
   return ((y - 0.5) * log(y) - y) + (HALF_LOG_2PI + s);
 }
 
-// log Gamma(x) for x > 0 (returns +inf at 0 and NaN for x < 0 or NaN).
-DUST2_HD double lgamma(double x) {
+// log Gamma(x) for x > 0 (returns +inf at 0 and NaN for x < 0 or NaN),
+// computed.
+DUST2_HD double lgamma_nontable(double x) {
   if (is_nan(x) || x < 0) {
     return quiet_nan();
   }
@@ -283,6 +419,46 @@ DUST2_HD double lgamma(double x) {
     y = y + 1.0;
   }
   return lgamma_stirling(y) - log(prod);
+}
+
+// log(k!) for k = 0 .. LF_TABLE_MAX in device memory (8 MiB), filled once
+// per device with lgamma_nontable(k + 1) by the same code, so reading the
+// table returns exactly what computing would.  Each translation unit
+// holds its own pointer (no relocatable device code); it stays null, and
+// lgamma computes, until the host binds it.
+constexpr int LF_TABLE_MAX = 1 << 20;
+#if defined(__CUDACC__)
+static __constant__ const double* lf_table_ptr = nullptr;
+#endif
+
+// x as an int if x is an integer in [1, 2^21), else -1 (on the bits).
+DUST2_HD int small_integer(double x) {
+  const std::uint64_t u = bits_of(x);
+  const int e = static_cast<int>(u >> 52) - 1023;  // sign set: e > 1023
+  if (e < 0 || e > 20) {
+    return -1;
+  }
+  const std::uint64_t m = (u & 0x000fffffffffffffull) | 0x0010000000000000ull;
+  const int sh = 52 - e;
+  if (m & ((1ull << sh) - 1)) {
+    return -1;
+  }
+  return static_cast<int>(m >> sh);
+}
+
+// log Gamma(x), as lgamma_nontable; on the device integer arguments up to
+// LF_TABLE_MAX + 1 are read from the table.
+DUST2_HD double lgamma(double x) {
+#if defined(__CUDA_ARCH__)
+  const double* t = lf_table_ptr;
+  if (t != nullptr) {
+    const int k = small_integer(x);
+    if (k >= 1 && k <= LF_TABLE_MAX + 1) {
+      return t[k - 1];
+    }
+  }
+#endif
+  return lgamma_nontable(x);
 }
 
 // log(k!) for an integer-valued k >= 0.

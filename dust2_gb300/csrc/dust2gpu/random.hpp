@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "math.hpp"
 
 namespace dust2gpu {
 namespace random {
@@ -82,7 +83,9 @@ DUST2_HD double random_real(rng_state& s) {
   if (s.deterministic) {
     return 0.5;
   }
-  return static_cast<double>(next(s) >> 11) * 0x1.0p-53;
+  // same value as static_cast<double>(next(s) >> 11) * 2^-53, built on
+  // the integer pipe
+  return math::u53_to_unit(next(s) >> 11);
 }
 
 // Advance a stream by 2^128 draws.  The characteristic-polynomial

@@ -50,10 +50,15 @@ struct system_view {
   bool deterministic;
 };
 
+// Steps of one launch whose zero_every test is precomputed per block.
+constexpr int ZERO_STEPS_CACHED = 64;
+
 template <typename T>
 struct shared_smem {
   alignas(16) unsigned char shared_buf[sizeof(typename T::shared_state)];
   zero_every_spec zero;
+  // bit i of zero_steps[e]: fmod(time + i * dt, period[e]) == 0
+  std::uint64_t zero_steps[ZERO_EVERY_MAX];
 
   __device__ const typename T::shared_state& shared() const {
     return *reinterpret_cast<const typename T::shared_state*>(shared_buf);
@@ -62,6 +67,33 @@ struct shared_smem {
     block_load(reinterpret_cast<typename T::shared_state*>(shared_buf),
                v.shared + group);
     block_load(&zero, v.zero_every + group);
+  }
+  // Evaluate the zero_every test of the first ZERO_STEPS_CACHED steps
+  // once per block instead of once per particle and step (warp 0, one
+  // step per lane; the expression is the one run_particle would use).
+  // Called by every thread, before the barrier that follows load(); tiles
+  // are whole warps (a multiple of 32 threads), so warp 0 is complete.
+  __device__ void load_zero_steps(const system_view<T>& v, int group,
+                                  double time, double dt, int n_steps) {
+    if (threadIdx.x >= 32) {
+      return;
+    }
+    const zero_every_spec& z = v.zero_every[group];
+    const int lane = threadIdx.x;
+    for (int e = 0; e < z.n; ++e) {
+      std::uint64_t mask = 0;
+      for (int base = 0; base < ZERO_STEPS_CACHED && base < n_steps;
+           base += 32) {
+        const int i = base + lane;
+        const double t = time + static_cast<double>(i) * dt;
+        const bool hit = i < n_steps && fmod(t, z.period[e]) == 0;
+        mask |= static_cast<std::uint64_t>(__ballot_sync(0xffffffffu, hit))
+          << base;
+      }
+      if (lane == 0) {
+        zero_steps[e] = mask;
+      }
+    }
   }
 };
 
@@ -87,11 +119,16 @@ __device__ __forceinline__ void store_state(const system_view<T>& v, int k,
   }
 }
 
+// Reset the zero_every entries due at step `step` (time `time`): the
+// first ZERO_STEPS_CACHED steps read the block's precomputed masks.
 template <typename T>
-__device__ __forceinline__ void apply_zero_every(const zero_every_spec& z,
-                                                 double time, double* x) {
+__device__ __forceinline__ void apply_zero_every(
+    const zero_every_spec& z, const std::uint64_t* zero_steps, int step,
+    double time, double* x) {
   for (int i = 0; i < z.n; ++i) {
-    if (fmod(time, z.period[i]) == 0) {
+    const bool hit = step < ZERO_STEPS_CACHED ?
+      ((zero_steps[i] >> step) & 1) != 0 : fmod(time, z.period[i]) == 0;
+    if (hit) {
 #pragma unroll
       for (int s = 0; s < T::n_state_max; ++s) {
         if (z.has(i, s)) {
@@ -102,26 +139,23 @@ __device__ __forceinline__ void apply_zero_every(const zero_every_spec& z,
   }
 }
 
-// Advance one particle n_steps; on return the state is in x.
+// Advance one particle n_steps; on return the state is in x.  The
+// reference swaps the two state pointers after each step; since `update`
+// writes every entry of `state_next`, copying y back into x (register
+// moves) is equivalent and keeps a single inlined copy of `update` in the
+// loop (the samplers make it large; instruction-cache misses showed up as
+// "no instruction" stalls when the loop held three copies).
 template <typename T>
 __device__ __forceinline__ void run_particle(
     double time, double dt, int n_steps,
     const typename T::shared_state& shared,
     typename T::internal_state& internal, const zero_every_spec& z,
-    random::rng_state& rng, double* x, double* y) {
-  int i = 0;
-  for (; i + 1 < n_steps; i += 2) {
-    const double t0 = time + static_cast<double>(i) * dt;
-    apply_zero_every<T>(z, t0, x);
-    T::update(t0, dt, x, shared, internal, rng, y);
-    const double t1 = time + static_cast<double>(i + 1) * dt;
-    apply_zero_every<T>(z, t1, y);
-    T::update(t1, dt, y, shared, internal, rng, x);
-  }
-  if (i < n_steps) {
-    const double t0 = time + static_cast<double>(i) * dt;
-    apply_zero_every<T>(z, t0, x);
-    T::update(t0, dt, x, shared, internal, rng, y);
+    const std::uint64_t* zero_steps, random::rng_state& rng, double* x,
+    double* y) {
+  for (int i = 0; i < n_steps; ++i) {
+    const double t = time + static_cast<double>(i) * dt;
+    apply_zero_every<T>(z, zero_steps, i, t, x);
+    T::update(t, dt, x, shared, internal, rng, y);
 #pragma unroll
     for (int s = 0; s < T::n_state_max; ++s) {
       x[s] = y[s];
@@ -155,6 +189,7 @@ __global__ void k_run(system_view<T> v, double time, double dt, int n_steps) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
   sm.load(v, tl.group);
+  sm.load_zero_steps(v, tl.group, time, dt, n_steps);
   __syncthreads();
   if (static_cast<int>(threadIdx.x) >= tl.count) {
     return;
@@ -165,8 +200,8 @@ __global__ void k_run(system_view<T> v, double time, double dt, int n_steps) {
   double x[T::n_state_max];
   double y[T::n_state_max];
   load_state<T>(v, k, x);
-  run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero, rng, x,
-                  y);
+  run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
+                  sm.zero_steps, rng, x, y);
   store_state<T>(v, k, x);
   store_rng(v.rng, v.stride, k, rng);
   capture_error(v.errors, v.any_error, k, rng);

@@ -12,6 +12,7 @@
 #include "continuous.cuh"
 #include "discrete.cuh"
 #include "filter.cuh"
+#include "lf_table.hpp"
 #include "registry.hpp"
 
 namespace dust2gpu {
@@ -46,6 +47,7 @@ system_api* create_system(const double* pars, int n_groups,
                           double dt, const ode_control& control,
                           const std::vector<std::uint64_t>& rng_words,
                           bool deterministic, int tile_size) {
+  bind_lf_table();
   auto shared = build_shared_groups<T>(pars, n_groups);
   if constexpr (is_continuous<T>()) {
     return new continuous_system<T>(std::move(shared), time, control,
@@ -71,6 +73,7 @@ filter_api* create_filter(const double* pars, int n_groups,
       std::string("Can't create filter; the '") + T::name +
       "' system does not have 'compare_data' support");
   } else {
+    bind_lf_table();
     auto shared = build_shared_groups<T>(pars, n_groups);
     // Split the stream block (r/discrete/filter.hpp:63-75): per group the
     // first 2 streams go to the filter, the rest to the particles.

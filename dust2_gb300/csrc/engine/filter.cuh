@@ -129,6 +129,7 @@ __global__ void k_step_compare(system_view<T> v, filter_view f, double time,
     return;
   }
   sm.load(v, tl.group);
+  sm.load_zero_steps(v, tl.group, time, dt, n_steps);
   __syncthreads();
   const bool valid = static_cast<int>(threadIdx.x) < tl.count;
   double logw = 0;
@@ -139,8 +140,8 @@ __global__ void k_step_compare(system_view<T> v, filter_view f, double time,
     double x[T::n_state_max];
     double y[T::n_state_max];
     load_state<T>(v, k, x);
-    run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero, rng,
-                    x, y);
+    run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
+                    sm.zero_steps, rng, x, y);
     const auto& d = data[n_groups_data == 1 ? 0 : tl.group];
     logw = T::compare_data(time_compare, x, d, sm.shared(), internal, rng);
     store_state<T>(v, k, x);

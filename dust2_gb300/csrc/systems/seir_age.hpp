@@ -167,6 +167,8 @@ struct seir_age {
     }
     const real_type p_EI = 1 - math::exp(-shared.sigma * dt);
     const real_type p_IR = 1 - math::exp(-shared.gamma * dt);
+    // one age per iteration, not unrolled: the body holds three samplers
+#pragma unroll 1
     for (int a = 0; a < n_age; ++a) {
       real_type acc = 0;
       for (int b = 0; b < n_age; ++b) {

@@ -68,6 +68,28 @@ def seir_plist(r0_values, seed=7):
              "I0": 1, "contact": c.ravel()} for r in r0_values]
 
 
+def seir_batched(simulate, n_groups=32, n_particles=8192, seed=3,
+                 n_obs=365):
+    """Age-structured SEIR filter: 16 ages, contact matrix from seed 7,
+    sigma = 0.2, gamma = 0.1, R0 ~ U(1.2, 3) per group, dt = 0.25,
+    32 groups x 8192 particles; 365 daily observations of total incidence
+    per group simulated from seed 3 plus negative-binomial (size 20)
+    observation noise."""
+    rs = np.random.default_rng(seed)
+    r0 = rs.uniform(1.2, 3.0, n_groups)
+    plist = seir_plist(r0)
+    flat = pack("seir_age", plist)
+    times = np.arange(1, n_obs + 1, dtype=float)
+    sim = simulate("seir_age", flat, n_groups, 1, 0.25, seed, times)
+    inc = np.asarray(sim).reshape(times.size, n_groups, 96)[:, :, 80:96]
+    mu = inc.sum(axis=2) + 1e-6
+    size = 20.0
+    data = rs.negative_binomial(size, size / (size + mu)).astype(float)
+    return {"pars": flat, "plist": plist, "times": times, "data": data,
+            "dt": 0.25, "n_particles": [n_particles] * n_groups,
+            "seed": seed}
+
+
 def sirode_batched(n_instances=262144, seed=3):
     """dopri5 workload: beta ~ U(0.1, 0.5), gamma ~ U(0.05, 0.2), N = 1e6,
     I0 ~ U(1, 100); one parameter group per instance."""
