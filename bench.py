@@ -59,7 +59,10 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--workload", default="sir_batched",
-                   choices=["sir_batched", "sir_small", "seir_batched"])
+                   choices=["sir_batched", "sir_small", "seir_batched",
+                            "serve_seir"])
+    p.add_argument("--hbm-budget", type=float, default=16e9,
+                   help="device memory budget of the likelihood server")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU sample")
@@ -394,6 +397,169 @@ def gpu_arm(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def percentile(x, q):
+    return float(np.percentile(np.asarray(x, dtype=float), q))
+
+
+def serve_arm(args, rank, world, local):
+    """Served likelihoods vs the plain path on the serving workload.
+
+    `--steps K` is the number of requests per client (each client is an
+    MCMC chain: one request outstanding, the next after its result and an
+    exponential think time); `--warmup W` warm-up requests run first on a
+    separate session.  Served: every client's session is open on one
+    likelihood server and clients submit and wait from their own threads
+    in real time.  Plain: the same requests, in arrival order, one by one
+    through dust_likelihood_run on one-group filters (service times
+    measured; the arrival process is replayed against the single plain
+    executor, which is serial, to get each request's queueing delay).
+    Both arms include host parameters in and host log-likelihoods out."""
+    import heapq
+
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    import dust2_gb300 as d
+    from dust2_gb300 import workloads
+
+    rounds = args.steps
+    w = workloads.serving_clients(gpu_simulate_factory(), rounds=rounds)
+    clients = w["clients"]
+    C = len(clients)
+    gen = d.seir_age()
+    server = d.dust_likelihood_server(gen, hbm_budget=args.hbm_budget,
+                                      max_sessions=2 * C)
+    # warm-up (module load, first launches) on a separate session
+    c0 = clients[0]
+    warm = server.open(c0["pars"][0], c0["data"], 512, dt=w["dt"], seed=1)
+    for _ in range(args.warmup):
+        server.likelihood(warm, c0["pars"][0])
+    server.close(warm)
+    ids = [server.open(c["pars"][0], c["data"], c["n_particles"], dt=w["dt"],
+                       seed=c["seed"]) for c in clients]
+    server.set_timing(True)
+    st0 = server.stats()
+    served_ll = [[None] * rounds for _ in range(C)]
+    served_lat = []
+    lock = threading.Lock()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    t_end = [0.0] * C
+
+    def client(i):
+        c = clients[i]
+        delay = t0 + w["first_arrival"][i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        for r in range(rounds):
+            ticket = server.submit(ids[i], c["pars"][r])
+            ll, lat = server.wait(ticket)
+            with lock:
+                served_ll[i][r] = ll
+                served_lat.append(lat)
+            t_end[i] = time.perf_counter()
+            if r + 1 < rounds:
+                time.sleep(w["think"][i, r])
+
+    threads = [threading.Thread(target=client, args=(i,)) for i in range(C)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    served_s = max(t_end) - t0
+    clock_info = clocks.stop()
+    st = server.stats()
+    total_ps = rounds * sum(c["particle_steps"] for c in clients)
+    served_value = total_ps / served_s
+    step_ms = st["step_kernel_ms"] - st0["step_kernel_ms"]
+    launches = int(st["kernel_launches"] - st0["kernel_launches"])
+    server.free()
+
+    # plain arm
+    objs = [d.dust_filter_create(gen, 0, c["data"],
+                                 n_particles=c["n_particles"], dt=w["dt"],
+                                 seed=c["seed"]) for c in clients]
+    wobj = d.dust_filter_create(gen, 0, c0["data"], n_particles=512,
+                                dt=w["dt"], seed=1)
+    for _ in range(args.warmup):
+        d.dust_likelihood_run(wobj, c0["pars"][0])
+    heap = [(float(w["first_arrival"][i]), i, 0) for i in range(C)]
+    heapq.heapify(heap)
+    now = 0.0
+    plain_lat = []
+    plain_ll = [[None] * rounds for _ in range(C)]
+    service = []
+    while heap:
+        arrival, i, r = heapq.heappop(heap)
+        start = max(now, arrival)
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        ll = d.dust_likelihood_run(objs[i], clients[i]["pars"][r])
+        svc = time.perf_counter() - a
+        plain_ll[i][r] = float(np.ravel(ll)[0])
+        service.append(svc)
+        now = start + svc
+        plain_lat.append(now - arrival)
+        if r + 1 < rounds:
+            heapq.heappush(heap, (now + float(w["think"][i, r]), i, r + 1))
+    plain_s = now
+    plain_value = total_ps / plain_s
+    same = all(np.array_equal(np.array(a, dtype=float),
+                              np.array(b, dtype=float))
+               for a, b in zip(served_ll, plain_ll))
+
+    ops = FP64_OPS_PER_PARTICLE_STEP.get("seir_batched")
+    peak = fp64_peak_tflops()
+    in_kernel_rate = total_ps / (step_ms * 1e-3) if step_ms > 0 else None
+    achieved = (ops * in_kernel_rate / 1e12
+                if ops is not None and in_kernel_rate else None)
+    n_par = gen.n_pars
+    line = {
+        "metric": "served filter particle-steps/s",
+        "value": served_value, "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": rounds, "warmup": args.warmup,
+        "ms_per_step": served_s * 1e3 / rounds, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (simulated by the model, seeded)",
+        "config": {"workload": "serve_seir", "clients": C,
+                   "requests": C * rounds, "arrival_rate_per_s": w["rate"],
+                   "particles": [c["n_particles"] for c in clients],
+                   "particle_steps": total_ps,
+                   "hbm_budget_bytes": args.hbm_budget,
+                   "l2": "not flushed: a continuous request stream",
+                   "parallelism": "1 GPU, one server"},
+        "latency_s": {"served": {"p50": percentile(served_lat, 50),
+                                 "p99": percentile(served_lat, 99)},
+                      "plain": {"p50": percentile(plain_lat, 50),
+                                "p99": percentile(plain_lat, 99)}},
+        "plain": {"value": plain_value, "unit": "particle-steps/s",
+                  "seconds": plain_s,
+                  "mean_service_s": float(np.mean(service))},
+        "served_over_plain": served_value / plain_value,
+        "results_equal_plain": bool(same),
+        "server": {k: st[k] for k in ("device_steps", "requests_done",
+                                      "max_running", "particle_capacity")},
+        "e2e": {"value": served_value, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": C * n_par * 8,
+                "d2h_bytes_per_step": C * 8},
+        "gpu_launches": launches,
+        "clocks": clock_info,
+        "roofline": {
+            "bound": "fp64", "kernel": "k_served_step_compare<seir_age>",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": None if achieved is None else achieved / peak,
+            "traffic": None,
+            "step_kernel_share": step_ms * 1e-3 / served_s,
+            "flops_basis": "executed FP64 ops per particle-step of the "
+                           "SEIR step kernel (ncu, seir_batched)"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(args, rank, world):
     """The CPU implementation of the path on the host cores (the oracle
     port of dust2's engine; dust2's own sources are not present on the
@@ -458,6 +624,9 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         reference_arm(args, rank, world)
+    elif args.workload == "serve_seir":
+        if rank == 0:
+            serve_arm(args, rank, world, local)
     else:
         gpu_arm(args, rank, world, local)
 

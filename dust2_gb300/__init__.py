@@ -4,10 +4,10 @@ csrc/ (C ABI: include/dust2_gb300.h)."""
 
 from ._lib import DustError, device_count
 from .interface import (
-    DustLikelihood, DustSystem, Generator, dust_filter_create,
+    DustLikelihood, DustServer, DustSystem, Generator, dust_filter_create,
     dust_filter_data, dust_likelihood_last_state, dust_likelihood_rng_state,
     dust_likelihood_run, dust_likelihood_serial_fallbacks,
-    dust_likelihood_set_rng_state, dust_ode_control,
+    dust_likelihood_server, dust_likelihood_set_rng_state, dust_ode_control,
     dust_system_compare_data, dust_system_create, dust_system_internals,
     dust_system_reorder, dust_system_rng_state, dust_system_run_to_time,
     dust_system_set_rng_state, dust_system_set_state,
@@ -17,11 +17,12 @@ from .interface import (
     scale_log_weights, seir_age, sir, sir_cases, sirode, walk)
 
 __all__ = [
-    "DustError", "DustLikelihood", "DustSystem", "Generator",
+    "DustError", "DustLikelihood", "DustServer", "DustSystem", "Generator",
     "device_count", "dust_filter_create", "dust_filter_data",
     "dust_likelihood_last_state", "dust_likelihood_rng_state",
     "dust_likelihood_run", "dust_likelihood_serial_fallbacks",
-    "dust_likelihood_set_rng_state", "dust_ode_control",
+    "dust_likelihood_server", "dust_likelihood_set_rng_state",
+    "dust_ode_control",
     "dust_system_compare_data", "dust_system_create",
     "dust_system_internals", "dust_system_reorder", "dust_system_rng_state",
     "dust_system_run_to_time", "dust_system_set_rng_state",

@@ -132,7 +132,31 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_int32]),
     "dust2_gb300_filter_kernel_times": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p, c_i64_p, c_double_p, c_i64_p]),
+    "dust2_gb300_server_create": (ctypes.c_int, [
+        ctypes.c_char_p, ctypes.c_double, ctypes.c_size_t, c_void_pp]),
+    "dust2_gb300_server_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "dust2_gb300_server_capacity": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, c_size_p, c_size_p]),
+    "dust2_gb300_server_open": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, ctypes.c_size_t, ctypes.c_double,
+        c_double_p, ctypes.c_size_t, c_double_p, ctypes.c_double, c_u64_p,
+        ctypes.c_size_t, c_i64_p]),
+    "dust2_gb300_server_submit": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64, c_double_p, c_i64_p]),
+    "dust2_gb300_server_wait": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, c_double_p,
+        c_double_p]),
+    "dust2_gb300_server_close": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64]),
+    "dust2_gb300_server_rng_state": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int64, c_u64_p]),
+    "dust2_gb300_server_set_timing": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32]),
+    "dust2_gb300_server_stats": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, ctypes.c_size_t]),
 }
+
+PENDING = 2
 
 _lib = None
 

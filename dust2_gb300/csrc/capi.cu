@@ -31,6 +31,10 @@ struct dust2_gb300_filter {
   std::vector<int> last_index_group;
 };
 
+struct dust2_gb300_server {
+  std::unique_ptr<dust2gpu::engine::server_api> impl;
+};
+
 namespace dust2gpu {
 namespace engine {
 
@@ -188,6 +192,27 @@ system_api& sysref(dust2_gb300_system* sys) {
 filter_api& filref(dust2_gb300_filter* f) {
   need(f != nullptr && f->impl != nullptr, "Invalid filter handle");
   return *f->impl;
+}
+
+dust2gpu::engine::server_api& servref(dust2_gb300_server* s) {
+  need(s != nullptr && s->impl != nullptr, "Invalid server handle");
+  return *s->impl;
+}
+
+// r/helpers.hpp check_time_sequence(require_later = true), as for filters
+void check_data_times(double time_start, const double* time, size_t n_time) {
+  need(time != nullptr && n_time >= 1,
+       "Expected 'data' to have at least one row");
+  if (time[0] < time_start) {
+    char buf[200];
+    std::snprintf(buf, sizeof(buf),
+                  "'time_start' (%g) is later than the first time in "
+                  "'data' (%g)", time_start, time[0]);
+    throw std::runtime_error(buf);
+  }
+  for (std::size_t i = 1; i < n_time; ++i) {
+    need(time[i] > time[i - 1], "Values in 'time' must be increasing");
+  }
 }
 
 }  // namespace
@@ -744,6 +769,108 @@ int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
     filref(filter).kernel_times(step_ms, &a, run_ms, &b);
     *n_step_launches = a;
     *n_runs = b;
+  });
+}
+
+int dust2_gb300_server_create(const char* name, double hbm_budget_bytes,
+                              size_t max_sessions,
+                              dust2_gb300_server** out) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    need(max_sessions >= 1 && max_sessions <= (1u << 20),
+         "'max_sessions' must be between 1 and 2^20");
+    const auto* f = dust2gpu::engine::find_system(name);
+    auto* impl = f->create_server(hbm_budget_bytes,
+                                  static_cast<int>(max_sessions));
+    *out = new dust2_gb300_server{
+      std::unique_ptr<dust2gpu::engine::server_api>(impl)};
+  });
+}
+
+int dust2_gb300_server_free(dust2_gb300_server* server) {
+  return guard([&] { delete server; });
+}
+
+int dust2_gb300_server_capacity(dust2_gb300_server* server,
+                                size_t* n_particles, size_t* n_sessions,
+                                size_t* n_observations) {
+  return guard([&] {
+    servref(server).capacity(n_particles, n_sessions, n_observations);
+  });
+}
+
+int dust2_gb300_server_open(dust2_gb300_server* server, const double* pars,
+                            size_t n_particles, double time_start,
+                            const double* time, size_t n_time,
+                            const double* data, double dt,
+                            const uint64_t* seed, size_t seed_len,
+                            int64_t* session) {
+  return guard([&] {
+    auto& srv = servref(server);
+    need(session != nullptr && pars != nullptr && data != nullptr,
+         "NULL argument");
+    need(n_particles >= 1 && n_particles < (1u << 29),
+         "'n_particles' must be at least 1");
+    need(dt > 0, "Expected 'dt' to be greater than 0");
+    check_data_times(time_start, time, n_time);
+    std::size_t cap_particles, cap_sessions, cap_obs;
+    srv.capacity(&cap_particles, &cap_sessions, &cap_obs);
+    need(n_particles <= cap_particles && n_time <= cap_obs,
+         "This session needs more device memory than the server's budget");
+    auto words = seed_streams(seed, seed_len, n_particles + 2);
+    *session = srv.open_session(pars, static_cast<int>(n_particles),
+                                time_start, time, static_cast<int>(n_time),
+                                data, dt, std::move(words));
+  });
+}
+
+int dust2_gb300_server_submit(dust2_gb300_server* server, int64_t session,
+                              const double* pars, int64_t* ticket) {
+  return guard([&] {
+    need(ticket != nullptr, "ticket is NULL");
+    *ticket = servref(server).submit(session, pars);
+  });
+}
+
+int dust2_gb300_server_wait(dust2_gb300_server* server, int64_t ticket,
+                            double timeout, double* log_likelihood,
+                            double* latency) {
+  int status = DUST2_GB300_OK;
+  const int ret = guard([&] {
+    need(log_likelihood != nullptr && latency != nullptr, "NULL argument");
+    std::string error;
+    status = servref(server).wait(ticket, timeout, log_likelihood, latency,
+                                  &error);
+    if (status == 1) {
+      throw std::runtime_error(error);
+    }
+  });
+  return ret != DUST2_GB300_OK ? ret :
+    (status == 2 ? DUST2_GB300_PENDING : DUST2_GB300_OK);
+}
+
+int dust2_gb300_server_close(dust2_gb300_server* server, int64_t session) {
+  return guard([&] { servref(server).close_session(session); });
+}
+
+int dust2_gb300_server_rng_state(dust2_gb300_server* server, int64_t session,
+                                 uint64_t* out) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    servref(server).session_rng_state(session, out);
+  });
+}
+
+int dust2_gb300_server_set_timing(dust2_gb300_server* server,
+                                  int32_t enable) {
+  return guard([&] { servref(server).set_timing(enable != 0); });
+}
+
+int dust2_gb300_server_stats(dust2_gb300_server* server, double* out,
+                             size_t n) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    servref(server).stats(out, static_cast<int>(std::min<size_t>(n, 64)));
   });
 }
 

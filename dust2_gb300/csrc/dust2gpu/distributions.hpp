@@ -51,11 +51,12 @@ constexpr int BINV_MAX_X = 110;
 // The recurrence f(x) = f(x-1) ((n+1) s / x - s), s = p/q, uses 1/x from
 // a table, and s from a reciprocal, so the loop has no FP64 division.
 // u stays >= 0 (it only loses a smaller r), so `u > r` is a bit compare.
-DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
-  const double q = 1.0 - p;
-  const double s = p * math::rcp(q);
+// The terms that depend on p only (q = 1 - p, s = p * rcp(q), log q) are
+// arguments, so that a prepared probability can supply them.
+DUST2_HD double binomial_inversion(rng_state& rng, double n, double p,
+                                   double q, double s, double logq) {
   const double a = (n + 1.0) * s;
-  const double r0 = math::exp(n * math::log(q));  // q^n
+  const double r0 = math::exp(n * logq);  // q^n
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
     double r = r0;
     double u = random_real(rng);
@@ -76,11 +77,27 @@ DUST2_HD double binomial_inversion(rng_state& rng, double n, double p) {
   return math::quiet_nan();
 }
 
+// log(p / q) of BTRS's acceptance test, computed when first needed ...
+struct btrs_lpq_lazy {
+  double p, q;
+  DUST2_HD double operator()() const {
+    return math::log(p * math::rcp(q));
+  }
+};
+// ... or supplied by a prepared probability (the same value).
+struct btrs_lpq_ready {
+  double lpq;
+  DUST2_HD double operator()() const {
+    return lpq;
+  }
+};
+
 // Divisions by b, us, q and the hat denominator are multiplications by
 // reciprocals (math::rcp); us = 0 (u = -1/2 exactly) is rejected.  Here
 // n p >= 10 and q >= 1/2, so b > 6.8 and v_r > 0.3.
-DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
-  const double q = 1.0 - p;
+template <typename LPQ>
+DUST2_HD double binomial_btrs(rng_state& rng, double n, double p, double q,
+                              const LPQ& lpq_of) {
   const double spq = std::sqrt(n * p * q);
   const double b = 1.15 + 2.53 * spq;
   const double a = -0.0873 + 0.0248 * b + 0.01 * p;
@@ -110,7 +127,7 @@ DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
     }
     if (!have_setup) {
       alpha = (2.83 + 5.1 * inv_b) * spq;
-      lpq = math::log(p * math::rcp(q));
+      lpq = lpq_of();
       m = std::floor((n + 1.0) * p);
       h = math::log_factorial(m) + math::log_factorial(n - m);
       have_setup = true;
@@ -125,16 +142,24 @@ DUST2_HD double binomial_btrs(rng_state& rng, double n, double p) {
   return math::quiet_nan();
 }
 
+constexpr std::uint64_t BITS_MINUS_ZERO = 0x8000000000000000ull;
+constexpr std::uint64_t BITS_ONE = 0x3ff0000000000000ull;
+constexpr std::uint64_t BITS_HALF = 0x3fe0000000000000ull;
+constexpr std::uint64_t BITS_TEN = 0x4024000000000000ull;
+
+// n >= 0 and finite (-0 included), on the bits.
+DUST2_HD bool binomial_n_ok(std::uint64_t nb) {
+  return nb < 0x7ff0000000000000ull || nb == BITS_MINUS_ZERO;
+}
+
 // Binomial(n, p) for integer-valued n >= 0 and p in [0, 1].  The argument
 // checks are taken on the bit patterns, with the FP64 semantics of
 // !(n >= 0) || !finite(n) || !(p >= 0) || !(p <= 1) (so -0 is valid).
 DUST2_HD double binomial(rng_state& rng, double n, double p) {
   const std::uint64_t nb = math::bits_of(n);
   const std::uint64_t pb = math::bits_of(p);
-  constexpr std::uint64_t MINUS_ZERO = 0x8000000000000000ull;
-  const bool n_ok = nb < 0x7ff0000000000000ull || nb == MINUS_ZERO;
-  const bool p_ok = pb <= 0x3ff0000000000000ull || pb == MINUS_ZERO;
-  if (!n_ok || !p_ok) {
+  const bool p_ok = pb <= BITS_ONE || pb == BITS_MINUS_ZERO;
+  if (!binomial_n_ok(nb) || !p_ok) {
     set_error(rng, ERR_BINOMIAL_INVALID, n, p);
     return math::quiet_nan();
   }
@@ -144,16 +169,78 @@ DUST2_HD double binomial(rng_state& rng, double n, double p) {
   if ((nb << 1) == 0 || (pb << 1) == 0) {  // n == 0 || p == 0
     return 0;
   }
-  if (pb == 0x3ff0000000000000ull) {  // p == 1
+  if (pb == BITS_ONE) {  // p == 1
     return n;
   }
-  const bool flip = pb > 0x3fe0000000000000ull;  // p > 1/2
+  const bool flip = pb > BITS_HALF;  // p > 1/2
   const double pp = flip ? 1.0 - p : p;
+  const double q = 1.0 - pp;
   // n * pp < 10 (n * pp is positive and finite)
-  const bool small_mean = math::bits_of(n * pp) < 0x4024000000000000ull;
-  const double x = small_mean ? binomial_inversion(rng, n, pp) :
-    binomial_btrs(rng, n, pp);
+  double x;
+  if (math::bits_of(n * pp) < BITS_TEN) {
+    const double s = pp * math::rcp(q);
+    x = binomial_inversion(rng, n, pp, q, s, math::log(q));
+  } else {
+    x = binomial_btrs(rng, n, pp, q, btrs_lpq_lazy{pp, q});
+  }
   return flip ? n - x : x;
+}
+
+// A probability prepared for many Binomial draws (the same p for several
+// counts, as a system drawing one transition per age class does): the
+// terms of both samplers that depend on p alone, evaluated once by the
+// expressions binomial() uses, so binomial(rng, n, binomial_prepare(p))
+// returns exactly binomial(rng, n, p) and consumes the same draws.
+struct binomial_prob {
+  double p;     // as given
+  double pp;    // min(p, 1 - p)
+  double q;     // 1 - pp
+  double s;     // pp * rcp(q)
+  double logq;  // log(q)
+  double lpq;   // log(s)
+  std::uint64_t bits;
+  bool valid;
+  bool flip;
+};
+
+DUST2_HD binomial_prob binomial_prepare(double p) {
+  binomial_prob b{};
+  b.p = p;
+  b.bits = math::bits_of(p);
+  b.valid = b.bits <= BITS_ONE || b.bits == BITS_MINUS_ZERO;
+  b.flip = b.valid && b.bits > BITS_HALF;
+  b.pp = b.flip ? 1.0 - p : p;
+  if (b.valid && (b.bits << 1) != 0 && b.bits != BITS_ONE) {
+    b.q = 1.0 - b.pp;
+    b.s = b.pp * math::rcp(b.q);
+    b.logq = math::log(b.q);
+    b.lpq = math::log(b.s);
+  }
+  return b;
+}
+
+DUST2_HD double binomial(rng_state& rng, double n, const binomial_prob& b) {
+  const std::uint64_t nb = math::bits_of(n);
+  if (!binomial_n_ok(nb) || !b.valid) {
+    set_error(rng, ERR_BINOMIAL_INVALID, n, b.p);
+    return math::quiet_nan();
+  }
+  if (rng.deterministic) {
+    return n * b.p;
+  }
+  if ((nb << 1) == 0 || (b.bits << 1) == 0) {
+    return 0;
+  }
+  if (b.bits == BITS_ONE) {
+    return n;
+  }
+  double x;
+  if (math::bits_of(n * b.pp) < BITS_TEN) {
+    x = binomial_inversion(rng, n, b.pp, b.q, b.s, b.logq);
+  } else {
+    x = binomial_btrs(rng, n, b.pp, b.q, btrs_lpq_ready{b.lpq});
+  }
+  return b.flip ? n - x : x;
 }
 
 DUST2_HD double poisson_knuth(rng_state& rng, double lambda) {
@@ -222,7 +309,7 @@ DUST2_HD double poisson(rng_state& rng, double lambda) {
   if ((lb << 1) == 0) {
     return 0;
   }
-  return lb < 0x4024000000000000ull ? poisson_knuth(rng, lambda) :
+  return lb < BITS_TEN ? poisson_knuth(rng, lambda) :
     poisson_ptrs(rng, lambda);
 }
 

@@ -163,8 +163,34 @@ __device__ __forceinline__ void run_particle(
   }
 }
 
+// Pick a block size for a system: big states need more registers per
+// thread, so fewer threads per block keep occupancy sane.  Every kernel
+// over a system's particles runs with this block size.
 template <typename T>
-__global__ void k_initial(system_view<T> v, const int* active, double time) {
+constexpr int default_tile_size() {
+  return T::n_state_max > 32 ? 128 : 256;
+}
+
+// Blocks per SM the per-particle kernels of a system must fit, which caps
+// registers per thread at 65536 / (tile size * blocks): a system may
+// declare `static constexpr int min_blocks_per_sm`; the default, 2, allows
+// 128 registers at 256 threads and 255 at 128.
+template <typename T, typename = void>
+struct min_blocks_of {
+  static constexpr int value = 2;
+};
+template <typename T>
+struct min_blocks_of<T, std::void_t<decltype(T::min_blocks_per_sm)>> {
+  static constexpr int value = T::min_blocks_per_sm;
+};
+
+#define DUST2_PARTICLE_KERNEL(T)                                          \
+  __global__ void __launch_bounds__(default_tile_size<T>(),               \
+                                    min_blocks_of<T>::value)
+
+template <typename T>
+DUST2_PARTICLE_KERNEL(T) k_initial(system_view<T> v, const int* active,
+                                   double time) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
   sm.load(v, tl.group);
@@ -185,7 +211,8 @@ __global__ void k_initial(system_view<T> v, const int* active, double time) {
 }
 
 template <typename T>
-__global__ void k_run(system_view<T> v, double time, double dt, int n_steps) {
+DUST2_PARTICLE_KERNEL(T) k_run(system_view<T> v, double time, double dt,
+                               int n_steps) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
   sm.load(v, tl.group);
@@ -210,7 +237,7 @@ __global__ void k_run(system_view<T> v, double time, double dt, int n_steps) {
 // out[k] = compare_data(time, state_k, data[group or 0]); data is
 // [n_groups_data] of the system's data_type.
 template <typename T>
-__global__ void k_compare(system_view<T> v, double time,
+DUST2_PARTICLE_KERNEL(T) k_compare(system_view<T> v, double time,
                           const typename T::data_type* data,
                           int n_groups_data, double* out) {
   __shared__ shared_smem<T> sm;
@@ -233,13 +260,6 @@ __global__ void k_compare(system_view<T> v, double time,
   }
 }
 
-// Pick a block size for a system: big states need more registers per
-// thread, so fewer threads per block keep occupancy sane.
-template <typename T>
-int default_tile_size() {
-  return T::n_state_max > 32 ? 128 : 256;
-}
-
 // The device-resident discrete-time system.
 template <typename T>
 class discrete_system : public system_api {
@@ -260,6 +280,10 @@ public:
     time_(time), dt_(dt), deterministic_(deterministic) {
     if (static_cast<int>(shared_.size()) != layout_.n_groups) {
       throw std::runtime_error("shared state does not match group count");
+    }
+    if (layout_.tile_size > default_tile_size<T>()) {
+      // the kernels are compiled for at most this many threads per block
+      throw std::runtime_error("tile size above the system's block size");
     }
     for (std::size_t g = 1; g < shared_.size(); ++g) {
       const int n_g = T::n_state(shared_[g]);

@@ -14,6 +14,7 @@
 #include "filter.cuh"
 #include "lf_table.hpp"
 #include "registry.hpp"
+#include "served.cuh"
 
 namespace dust2gpu {
 namespace engine {
@@ -101,6 +102,18 @@ filter_api* create_filter(const double* pars, int n_groups,
 }
 
 template <typename T>
+server_api* create_server(double hbm_budget_bytes, int max_sessions) {
+  if constexpr (is_continuous<T>() || !has_compare_data<T>::value) {
+    throw std::runtime_error(
+      std::string("Can't serve likelihoods of the '") + T::name +
+      "' system: it has no discrete-time filter");
+  } else {
+    bind_lf_table();
+    return new served_engine<T>(hbm_budget_bytes, max_sessions);
+  }
+}
+
+template <typename T>
 struct registrar {
   system_factory factory;
   explicit registrar() {
@@ -110,6 +123,7 @@ struct registrar {
     factory.info_json = &system_info_json<T>;
     factory.create_system = &create_system<T>;
     factory.create_filter = &create_filter<T>;
+    factory.create_server = &create_server<T>;
     register_system(&factory);
   }
 };

@@ -94,7 +94,7 @@ struct filter_view {
 __global__ void k_filter_reset(filter_view f, int n_groups);
 
 template <typename T>
-__global__ void k_initial_flagged(system_view<T> v, const int* flag,
+DUST2_PARTICLE_KERNEL(T) k_initial_flagged(system_view<T> v, const int* flag,
                                   double time) {
   __shared__ shared_smem<T> sm;
   if (*flag == 0) {
@@ -117,17 +117,15 @@ __global__ void k_initial_flagged(system_view<T> v, const int* flag,
   capture_error(v.errors, v.any_error, k, rng);
 }
 
+// The per-tile work of k_step_compare, shared with the likelihood
+// server: advance each particle of tile `tl` n_steps from `time`, compare
+// it with `d` (this tile's data row), store its log weight, and reduce the
+// group's "any weight non-zero" flag and maximum log weight.
 template <typename T>
-__global__ void k_step_compare(system_view<T> v, filter_view f, double time,
-                               double dt, int n_steps, double time_compare,
-                               const typename T::data_type* data,
-                               int n_groups_data) {
-  __shared__ shared_smem<T> sm;
-  __shared__ double red[33];
-  const tile tl = v.tiles[blockIdx.x];
-  if (!f.active[tl.group]) {
-    return;
-  }
+__device__ __forceinline__ void step_compare_tile(
+    const system_view<T>& v, const filter_view& f, const tile& tl,
+    shared_smem<T>& sm, double* red, double time, double dt, int n_steps,
+    double time_compare, const typename T::data_type* d) {
   sm.load(v, tl.group);
   sm.load_zero_steps(v, tl.group, time, dt, n_steps);
   __syncthreads();
@@ -142,8 +140,7 @@ __global__ void k_step_compare(system_view<T> v, filter_view f, double time,
     load_state<T>(v, k, x);
     run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
                     sm.zero_steps, rng, x, y);
-    const auto& d = data[n_groups_data == 1 ? 0 : tl.group];
-    logw = T::compare_data(time_compare, x, d, sm.shared(), internal, rng);
+    logw = T::compare_data(time_compare, x, *d, sm.shared(), internal, rng);
     store_state<T>(v, k, x);
     store_rng(v.rng, v.stride, k, rng);
     capture_error(v.errors, v.any_error, k, rng);
@@ -161,10 +158,25 @@ __global__ void k_step_compare(system_view<T> v, filter_view f, double time,
   }
 }
 
+template <typename T>
+DUST2_PARTICLE_KERNEL(T) k_step_compare(system_view<T> v, filter_view f,
+                                        double time,
+                               double dt, int n_steps, double time_compare,
+                               const typename T::data_type* data,
+                               int n_groups_data) {
+  __shared__ shared_smem<T> sm;
+  __shared__ double red[33];
+  const tile tl = v.tiles[blockIdx.x];
+  if (!f.active[tl.group]) {
+    return;
+  }
+  step_compare_tile<T>(v, f, tl, sm, red, time, dt, n_steps, time_compare,
+                       data + (n_groups_data == 1 ? 0 : tl.group));
+}
+
 __global__ void k_weights(filter_view f);
 __global__ void k_group(filter_view f, int n_groups);
 __global__ void k_resample(filter_view f);
-__global__ void k_fallback(filter_view f);
 
 // Host-side description of the observation schedule.
 struct obs_step {

@@ -13,6 +13,7 @@
 #include "../dust2gpu/system.hpp"
 #include "api.hpp"
 #include "seeding.hpp"
+#include "server_api.hpp"
 
 namespace dust2gpu {
 namespace engine {
@@ -35,6 +36,8 @@ struct system_factory {
                                int n_groups_data, double dt,
                                const std::vector<std::uint64_t>& rng_words,
                                int tile_size);
+  // nullptr for systems without a filter (continuous time, no compare).
+  server_api* (*create_server)(double hbm_budget_bytes, int max_sessions);
 };
 
 void register_system(const system_factory* f);

@@ -167,6 +167,9 @@ struct seir_age {
     }
     const real_type p_EI = 1 - math::exp(-shared.sigma * dt);
     const real_type p_IR = 1 - math::exp(-shared.gamma * dt);
+    // the same two probabilities serve every age: prepare them once
+    const auto b_EI = random::binomial_prepare(p_EI);
+    const auto b_IR = random::binomial_prepare(p_IR);
     // one age per iteration, not unrolled: the body holds three samplers
 #pragma unroll 1
     for (int a = 0; a < n_age; ++a) {
@@ -177,8 +180,8 @@ struct seir_age {
       const real_type lambda = shared.beta * acc;
       const real_type p_SE = 1 - math::exp(-lambda * dt);
       const real_type n_SE = random::binomial(rng_state, S[a], p_SE);
-      const real_type n_EI = random::binomial(rng_state, E[a], p_EI);
-      const real_type n_IR = random::binomial(rng_state, I[a], p_IR);
+      const real_type n_EI = random::binomial(rng_state, E[a], b_EI);
+      const real_type n_IR = random::binomial(rng_state, I[a], b_IR);
       state_next[a] = S[a] - n_SE;
       state_next[n_age + a] = E[a] + n_SE - n_EI;
       state_next[2 * n_age + a] = I[a] + n_EI - n_IR;

@@ -959,3 +959,124 @@ def dust_likelihood_serial_fallbacks(obj):
     check(_lib.lib().dust2_gb300_filter_serial_fallbacks(obj.ptr,
                                                          ctypes.byref(n)))
     return n.value
+
+
+# ---------------------------------------------------------------------------
+# Likelihood server (continuous batching of many likelihood objects; no
+# counterpart in dust2, whose MCMC caller R/monty.R:90-317 runs one
+# dust_likelihood_run per chain and proposal)
+
+SERVER_STATS = ("device_steps", "particle_steps", "requests_done",
+                "resident_sessions", "sessions_waiting", "requests_queued",
+                "particle_capacity", "particles_in_use", "max_running",
+                "step_kernel_ms", "timed_steps", "kernel_launches")
+
+
+class DustServer:
+    """Serves filter likelihoods of many sessions (one per MCMC chain) on
+    one device: submit() queues a run at new parameters and returns at
+    once; wait() returns its log-likelihood.  A session is a one-group
+    likelihood object (dust_filter_create with n_groups = 1); its results
+    equal those of that object run on its own."""
+
+    def __init__(self, generator, hbm_budget=8e9, max_sessions=1024):
+        gen = _generator(generator)
+        if not gen.has_compare or gen.time_type == "continuous":
+            raise DustError(f"Can't serve likelihoods of the '{gen.name}' "
+                            "system")
+        self.generator = gen
+        handle = ctypes.c_void_p()
+        check(_lib.lib().dust2_gb300_server_create(
+            gen.name.encode(), float(hbm_budget), int(max_sessions),
+            ctypes.byref(handle)))
+        self._handle = handle
+
+    def __del__(self):
+        self.free()
+
+    def free(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.dust2_gb300_server_free(h)
+        self._handle = None
+
+    def capacity(self):
+        v = [ctypes.c_size_t() for _ in range(3)]
+        check(_lib.lib().dust2_gb300_server_capacity(
+            self._handle, *[ctypes.byref(x) for x in v]))
+        return {"n_particles": v[0].value, "n_sessions": v[1].value,
+                "n_observations": v[2].value}
+
+    def open(self, pars, data, n_particles, time_start=0, dt=None,
+             seed=None):
+        """A session with the arguments of dust_filter_create (one group)
+        and its first parameters; returns its id."""
+        gen = self.generator
+        n_particles = _scalar_size(n_particles, "n_particles")
+        if n_particles > self.capacity()["n_particles"]:
+            raise DustError("This session needs more device memory than the "
+                            "server's budget")
+        d = _prepare_data(data, None, False, gen)
+        if d["n_groups"] != 1:
+            raise DustError("A session has exactly one group")
+        dt = _check_dt(dt, gen)
+        flat = as_f64(gen.pack_pars(pars))
+        rows = as_f64(d["rows"])
+        times = as_f64(d["time"])
+        words = np.frombuffer(rng_streams(n_particles + 2, seed),
+                              dtype="<u8").astype(np.uint64)
+        sid = ctypes.c_int64()
+        check(_lib.lib().dust2_gb300_server_open(
+            self._handle, dptr(flat), n_particles, float(time_start),
+            dptr(times), times.size, dptr(rows), dt, uptr(words),
+            words.size, ctypes.byref(sid)))
+        return sid.value
+
+    def submit(self, session, pars=None):
+        flat = None if pars is None else as_f64(
+            self.generator.pack_pars(pars))
+        t = ctypes.c_int64()
+        check(_lib.lib().dust2_gb300_server_submit(
+            self._handle, int(session), dptr(flat), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout=None):
+        """(log-likelihood, latency in seconds); None if `timeout` seconds
+        pass first."""
+        ll = ctypes.c_double()
+        lat = ctypes.c_double()
+        rc = _lib.lib().dust2_gb300_server_wait(
+            self._handle, int(ticket), -1.0 if timeout is None else
+            float(timeout), ctypes.byref(ll), ctypes.byref(lat))
+        if rc == _lib.PENDING:
+            return None
+        check(rc)
+        return ll.value, lat.value
+
+    def likelihood(self, session, pars=None):
+        return self.wait(self.submit(session, pars))[0]
+
+    def close(self, session):
+        check(_lib.lib().dust2_gb300_server_close(self._handle,
+                                                  int(session)))
+
+    def rng_state(self, session, n_particles):
+        out = np.zeros(4 * (n_particles + 2), dtype=np.uint64)
+        check(_lib.lib().dust2_gb300_server_rng_state(
+            self._handle, int(session), uptr(out)))
+        return out.astype("<u8").tobytes()
+
+    def set_timing(self, enable):
+        check(_lib.lib().dust2_gb300_server_set_timing(self._handle,
+                                                       int(bool(enable))))
+
+    def stats(self):
+        out = np.zeros(len(SERVER_STATS))
+        check(_lib.lib().dust2_gb300_server_stats(self._handle, dptr(out),
+                                                  out.size))
+        return dict(zip(SERVER_STATS, out.tolist()))
+
+
+def dust_likelihood_server(generator, hbm_budget=8e9, max_sessions=1024):
+    """A likelihood server for a discrete-time system with compare_data."""
+    return DustServer(generator, hbm_budget, max_sessions)

@@ -90,6 +90,43 @@ def seir_batched(simulate, n_groups=32, n_particles=8192, seed=3,
             "seed": seed}
 
 
+def serving_clients(simulate, n_clients=64, rounds=2, seed=11, rate=200.0,
+                    n_days=365):
+    """Likelihood requests of concurrent MCMC chains on the age-structured
+    SEIR: one session per client with particles round(2^U(9, 15)) (log-
+    uniform in 512..32768) and U{50..365} days of data (simulated total
+    incidence from seed 11 plus negative-binomial noise, size 20); each
+    request a new R0 ~ U(1.2, 3).  Arrivals: the clients' first requests
+    form a Poisson stream at `rate` per second; after a result a client
+    waits an exponential time with mean n_clients / rate before its next
+    request (each chain has one request outstanding at a time)."""
+    rs = np.random.default_rng(seed)
+    r0 = rs.uniform(1.2, 3.0, n_clients)
+    plist = seir_plist(r0)
+    flat = pack("seir_age", plist)
+    times = np.arange(1, n_days + 1, dtype=float)
+    sim = simulate("seir_age", flat, n_clients, 1, 0.25, seed, times)
+    inc = np.asarray(sim).reshape(n_days, n_clients, 96)[:, :, 80:96]
+    mu = inc.sum(axis=2) + 1e-6
+    size = 20.0
+    data = rs.negative_binomial(size, size / (size + mu)).astype(float)
+    clients = []
+    for i in range(n_clients):
+        n = int(round(2 ** rs.uniform(9, 15)))
+        n_obs = int(rs.integers(50, 366))
+        seq = [dict(plist[i], R0=float(rs.uniform(1.2, 3.0)))
+               for _ in range(rounds)]
+        clients.append({
+            "n_particles": n,
+            "data": {"time": times[:n_obs], "incidence": data[:n_obs, i]},
+            "pars": seq, "seed": seed * 1000 + i,
+            "particle_steps": n * n_obs * 4})
+    first = np.cumsum(rs.exponential(1.0 / rate, n_clients))
+    think = rs.exponential(n_clients / rate, (n_clients, rounds))
+    return {"clients": clients, "first_arrival": first, "think": think,
+            "rate": rate, "dt": 0.25}
+
+
 def sirode_batched(n_instances=262144, seed=3):
     """dopri5 workload: beta ~ U(0.1, 0.5), gamma ~ U(0.05, 0.2), N = 1e6,
     I0 ~ U(1, 100); one parameter group per instance."""

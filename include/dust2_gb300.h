@@ -318,6 +318,89 @@ int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
                                     double* step_ms, int64_t* n_step_launches,
                                     double* run_ms, int64_t* n_runs);
 
+/* ---- likelihood server ---------------------------------------------------
+ *
+ * Continuous batching of filter likelihoods for many concurrent callers
+ * (MCMC chains).  dust2 has no counterpart: each chain calls
+ * dust_likelihood_run (R/interface-likelihood.R, filter.hpp:42-104) on
+ * its own object, one run at a time, from dust_likelihood_monty
+ * (R/monty.R:90-317).  Here each chain opens a session (its likelihood
+ * object: one parameter group, particle count, data and generator
+ * streams, kept on the device) and submits requests (a run at new
+ * parameters); the server runs all pending requests together, one
+ * observation per step of the device loop, admitting sessions as slots
+ * and memory under the HBM budget free up.  A request's result equals
+ * that of dust2_gb300_filter_run on a one-group filter created with the
+ * same parameters, data and seed, after the same earlier runs.
+ *
+ * Calls are thread safe; submit returns at once, wait blocks. */
+
+typedef struct dust2_gb300_server dust2_gb300_server;
+
+#define DUST2_GB300_PENDING 2
+
+/* A server for system `name` (a discrete-time system with compare_data)
+ * using at most hbm_budget_bytes of device memory for particles, data
+ * and per-session state, with at most max_sessions resident sessions. */
+int dust2_gb300_server_create(const char* name, double hbm_budget_bytes,
+                              size_t max_sessions,
+                              dust2_gb300_server** out);
+
+/* Stop the server: requests not yet started fail, running ones finish. */
+int dust2_gb300_server_free(dust2_gb300_server* server);
+
+/* Particles, sessions and observations the budget holds. */
+int dust2_gb300_server_capacity(dust2_gb300_server* server,
+                                size_t* n_particles, size_t* n_sessions,
+                                size_t* n_observations);
+
+/* Open a session: as dust2_gb300_filter_alloc with n_groups = 1 (pars one
+ * row of the parameter table; data n_time rows, time-major; seed as
+ * there).  The session becomes resident as soon as memory allows. */
+int dust2_gb300_server_open(dust2_gb300_server* server, const double* pars,
+                            size_t n_particles, double time_start,
+                            const double* time, size_t n_time,
+                            const double* data, double dt,
+                            const uint64_t* seed, size_t seed_len,
+                            int64_t* session);
+
+/* Queue one likelihood evaluation of `session`.  pars (one row; NaN keeps
+ * a value) updates the session's parameters first, as
+ * dust2_gb300_filter_update_pars does; NULL keeps them. */
+int dust2_gb300_server_submit(dust2_gb300_server* server, int64_t session,
+                              const double* pars, int64_t* ticket);
+
+/* Wait at most `timeout` seconds (negative: no limit) for a request:
+ * DUST2_GB300_OK with its log-likelihood and latency (seconds from submit
+ * to result), DUST2_GB300_ERROR if it failed (message as for particle
+ * errors of a filter run), DUST2_GB300_PENDING if not finished in time.
+ * A finished ticket is consumed. */
+int dust2_gb300_server_wait(dust2_gb300_server* server, int64_t ticket,
+                            double timeout, double* log_likelihood,
+                            double* latency);
+
+/* Close a session once its queued requests have run. */
+int dust2_gb300_server_close(dust2_gb300_server* server, int64_t session);
+
+/* Generator state of a session (waits until it is idle), in the layout of
+ * dust2_gb300_filter_rng_state for one group: 2 + n_particles streams. */
+int dust2_gb300_server_rng_state(dust2_gb300_server* server, int64_t session,
+                                 uint64_t* out);
+
+/* Enable (1) or disable (0) device timing of the step+compare kernel of
+ * every device step (CUDA events); resets the accumulated time. */
+int dust2_gb300_server_set_timing(dust2_gb300_server* server,
+                                  int32_t enable);
+
+/* Counters: [0] device steps (observations advanced), [1] particle-steps
+ * of started requests, [2] finished requests, [3] resident sessions,
+ * [4] sessions waiting for memory, [5] queued requests, [6] particle
+ * capacity, [7] particles in use, [8] most requests running at once,
+ * [9] step-kernel device time (ms, while timing), [10] timed device
+ * steps, [11] kernel launches.  Writes min(n, 12) values. */
+int dust2_gb300_server_stats(dust2_gb300_server* server, double* out,
+                             size_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -162,3 +162,23 @@ def test_invalid_handles_are_errors(built):
     assert "Invalid system handle" in _lib.last_error()
     assert lib.dust2_gb300_filter_run(None, None, None, 0, None) == 1
     assert "Invalid filter handle" in _lib.last_error()
+
+
+def test_server_validation_without_device(built):
+    lib = _lib.lib()
+    h = ctypes.c_void_p()
+    assert lib.dust2_gb300_server_create(b"nope", 1e8, 4,
+                                         ctypes.byref(h)) == 1
+    assert "Unknown system 'nope'" in _lib.last_error()
+    assert lib.dust2_gb300_server_create(b"sir", 1e8, 0,
+                                         ctypes.byref(h)) == 1
+    assert "'max_sessions'" in _lib.last_error()
+    assert lib.dust2_gb300_server_create(b"sirode", 1e8, 4,
+                                         ctypes.byref(h)) == 1
+    assert "Can't serve likelihoods of the 'sirode' system" in \
+        _lib.last_error()
+    t = ctypes.c_int64()
+    assert lib.dust2_gb300_server_submit(None, 1, None, ctypes.byref(t)) == 1
+    assert "Invalid server handle" in _lib.last_error()
+    with pytest.raises(d.DustError, match="Can't serve"):
+        d.dust_likelihood_server(d.walk())
