@@ -48,7 +48,22 @@ sys.path.insert(0, str(ROOT))
 # particle-step of the step+compare kernel, per workload, from the ncu SASS
 # counters of that kernel over a whole likelihood run (summaries under
 # profiles/).  A workload without an entry reports no achieved rate.
-FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 273.9}
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 273.9, "ode_batched": 761.7}
+# FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
+# unit, from the same captures: the pipe's own roofline (every instruction
+# takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
+FP64_PIPE_INST_PER_UNIT = {"sir_batched": 216.2, "ode_batched": 641.3}
+
+
+def pipe_roofline(workload, units_per_s, peak_tflops):
+    """Useful FP64-pipe thread instructions per second against the pipe's
+    peak (peak DFMA flops / 2)."""
+    n = FP64_PIPE_INST_PER_UNIT.get(workload)
+    if n is None or units_per_s is None:
+        return None
+    peak = peak_tflops * 1e12 / 2
+    return {"inst_per_unit": n, "achieved_inst_per_s": n * units_per_s,
+            "peak_inst_per_s": peak, "frac": n * units_per_s / peak}
 STEPS_PER_OBS = 4  # dt = 0.25, daily observations
 
 
@@ -60,7 +75,7 @@ def parse_args():
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--workload", default="sir_batched",
                    choices=["sir_batched", "sir_small", "seir_batched",
-                            "serve_seir"])
+                            "serve_seir", "ode_batched"])
     p.add_argument("--hbm-budget", type=float, default=16e9,
                    help="device memory budget of the likelihood server")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -364,6 +379,8 @@ def gpu_arm(args, rank, world, local):
             "peak_source": "measured in-process: DFMA-chain microbenchmark "
                            "(dust2_gb300_fp64_peak); MEASURED_PEAKS.json has no FP64 entry",
             "step_launch_ms": step_launch_ms,
+            "fp64_pipe": pipe_roofline(
+                args.workload, ps_per_launch / (step_launch_ms * 1e-3), peak),
             "step_share_of_run": step_ms.value / max(run_ms.value, 1e-12),
             "flops_basis": "executed FP64 ops per particle-step (ncu SASS "
                            "dadd+dmul+2*dfma)"}
@@ -560,6 +577,161 @@ def serve_arm(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def ode_alloc(w, seed=1):
+    """The batched sirode system through the C ABI (one group per
+    instance, rtol = atol = 1e-6)."""
+    import ctypes
+    from dust2_gb300 import _lib
+    ctl = _lib.OdeControl(10000, 1e-6, 1e-6, float(np.finfo(float).eps),
+                          float("inf"), None, 0, 0)
+    pars = _lib.as_f64(w["pars"])
+    words = np.array([seed], dtype=np.uint64)
+    h = ctypes.c_void_p()
+    _lib.check(_lib.lib().dust2_gb300_system_alloc(
+        b"sirode", _lib.dptr(pars), w["n_groups"], 1, 0.0, 1.0,
+        ctypes.byref(ctl), _lib.uptr(words), 1, 0, ctypes.byref(h)))
+    return h
+
+
+def ode_cpu(w, n_inst, threads):
+    from oracle import pyoracle
+    port = pyoracle.port()
+    gen_pars = 4
+    pars = np.asarray(w["pars"]).reshape(-1, gen_pars)[:n_inst].ravel()
+    t0 = time.perf_counter()
+    _, stats = port.ode_simulate("sirode", pars, n_inst, 1, 0.0, w["times"],
+                                 5, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return dt, int(stats[:, 0].sum())
+
+
+def ode_cpu_baseline(w, target_seconds):
+    from oracle import pyoracle
+    threads = pyoracle.port().max_threads()
+    n = 1024
+    t, steps = ode_cpu(w, n, threads)
+    while t < target_seconds / 4 and n < w["n_groups"]:
+        n = min(w["n_groups"], n * 4)
+        t, steps = ode_cpu(w, n, threads)
+    return {"value": steps / t, "unit": "dopri5 steps/s", "cores": threads,
+            "kind": "port",
+            "sample": f"instances 1-{n} of {w['n_groups']}, integrated "
+                      f"0..200 with {w['times'].size} outputs",
+            "seconds": t}
+
+
+def ode_arm(args, rank, world, local):
+    """Batched dopri5: 262,144 sirode instances integrated 0..200 with
+    output at every integer time (rtol = atol = 1e-6).  A step of the
+    benchmark is one simulate of every instance from t = 0; the metric
+    counts attempted dopri5 steps (accepted + rejected) per second."""
+    import ctypes
+
+    import torch
+    torch.cuda.set_device(local)
+    import __graft_entry__
+    __graft_entry__.build()
+    from dust2_gb300 import _lib, workloads
+
+    lib = _lib.lib()
+    w = workloads.sirode_batched()
+    G = w["n_groups"]
+    times = _lib.as_f64(w["times"])
+    h = ode_alloc(w)
+    n_out = times.size * G * 5
+    out = torch.empty(n_out, dtype=torch.float64, device="cuda")
+    stream_ptr = ctypes.c_void_p()
+    _lib.check(lib.dust2_gb300_system_stream(h, ctypes.byref(stream_ptr)))
+    ext = torch.cuda.ExternalStream(stream_ptr.value)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def run_once(device=True, host_out=None):
+        _lib.check(lib.dust2_gb300_system_set_time(h, 0.0))
+        _lib.check(lib.dust2_gb300_system_set_state_initial(h))
+        if device:
+            _lib.check(lib.dust2_gb300_system_simulate_device(
+                h, _lib.dptr(times), times.size,
+                ctypes.c_void_p(out.data_ptr())))
+        else:
+            _lib.check(lib.dust2_gb300_system_simulate(
+                h, _lib.dptr(times), times.size, None, 0,
+                _lib.dptr(host_out)))
+
+    for _ in range(args.warmup):
+        run_once()
+    ns = np.zeros(G, dtype=np.int64)
+    na = np.zeros(G, dtype=np.int64)
+    nr = np.zeros(G, dtype=np.int64)
+    ss = np.zeros(G)
+    er = np.zeros(G)
+    _lib.check(lib.dust2_gb300_system_internals(
+        h, _lib.dptr(ss), _lib.dptr(er), ns.ctypes.data_as(_lib.c_i64_p),
+        na.ctypes.data_as(_lib.c_i64_p), nr.ctypes.data_as(_lib.c_i64_p)))
+    steps = int(ns.sum())
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    elapsed = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        _lib.check(lib.dust2_gb300_system_set_time(h, 0.0))
+        _lib.check(lib.dust2_gb300_system_set_state_initial(h))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        _lib.check(lib.dust2_gb300_system_simulate_device(
+            h, _lib.dptr(times), times.size, ctypes.c_void_p(out.data_ptr())))
+        e1.record(ext)
+        torch.cuda.synchronize()
+        elapsed.append(e0.elapsed_time(e1))
+    clock_info = clocks.stop()
+    ms = float(np.mean(elapsed))
+    host = np.empty(n_out)
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run_once(device=False, host_out=host)
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e))
+    peak = fp64_peak_tflops()
+    ops = FP64_OPS_PER_PARTICLE_STEP.get("ode_batched")
+    achieved = None if ops is None else ops * steps / (ms * 1e-3) / 1e12
+    _lib.check(lib.dust2_gb300_system_free(h))
+    line = {
+        "metric": "dopri5 steps/s", "value": steps / (ms * 1e-3),
+        "unit": "dopri5 steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded parameters)",
+        "config": {"workload": "ode_batched", "instances": G,
+                   "outputs": int(times.size), "rtol": 1e-6, "atol": 1e-6,
+                   "dopri5_steps_per_step": steps,
+                   "accepted": int(na.sum()), "rejected": int(nr.sum()),
+                   "steps_per_instance": [int(ns.min()), int(ns.max())],
+                   "l2": "flushed (256 MB write) between timed steps; "
+                         "outputs 2.1 GB",
+                   "parallelism": "1 GPU"},
+        "e2e": {"value": steps / e2e_s, "unit": "dopri5 steps/s",
+                "h2d_bytes_per_step": times.size * 8,
+                "d2h_bytes_per_step": n_out * 8, "seconds_per_step": e2e_s},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clock_info,
+        "roofline": {"bound": "fp64", "kernel": "k_ode_run<sirode>",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": None if achieved is None else achieved / peak,
+                     "traffic": None,
+                     "fp64_pipe": pipe_roofline("ode_batched",
+                                                steps / (ms * 1e-3), peak),
+                     "flops_basis": "executed FP64 ops per attempted "
+                                    "dopri5 step (ncu SASS)"},
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = ode_cpu_baseline(w, args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
 def reference_arm(args, rank, world):
     """The CPU implementation of the path on the host cores (the oracle
     port of dust2's engine; dust2's own sources are not present on the
@@ -573,34 +745,95 @@ def reference_arm(args, rank, world):
     engine_build.build()
     from oracle import pyoracle
 
-    w = build_workload(args.workload, oracle_simulate())
     port = pyoracle.port()
     threads = port.max_threads()
-    base = cpu_baseline(w, args.cpu_seconds)
-    n_groups = int(base["sample"].split("-")[1].split(" ")[0])
+    metric, unit = "filter particle-steps/s", "particle-steps/s"
+    if args.workload == "ode_batched":
+        from dust2_gb300 import workloads
+        w = workloads.sirode_batched()
+        base = ode_cpu_baseline(w, args.cpu_seconds)
+        n_inst = int(base["sample"].split("-")[1].split(" ")[0])
+
+        def one():
+            t, steps = ode_cpu(w, n_inst, threads)
+            return t, steps
+        metric, unit = "dopri5 steps/s", "dopri5 steps/s"
+    elif args.workload == "serve_seir":
+        from dust2_gb300 import workloads
+        w = workloads.serving_clients(oracle_simulate(), rounds=1)
+        clients, base = serve_cpu_sample(w, args.cpu_seconds, threads)
+
+        def one():
+            return serve_cpu_run(w, clients, threads)
+        metric = "served filter particle-steps/s"
+    else:
+        w = build_workload(args.workload, oracle_simulate())
+        base = cpu_baseline(w, args.cpu_seconds)
+        n_groups = int(base["sample"].split("-")[1].split(" ")[0])
+
+        def one():
+            return run_cpu(w, n_groups, threads)
     for _ in range(args.warmup):
-        run_cpu(w, n_groups, threads)
+        one()
     times = []
     ps = None
     for _ in range(args.steps):
-        t, ps = run_cpu(w, n_groups, threads)
+        t, ps = one()
         times.append(t)
     t = float(np.mean(times))
     value = ps / t
     line = {
-        "impl": "reference", "metric": "filter particle-steps/s",
-        "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "impl": "reference", "metric": metric,
+        "value": value, "unit": unit, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (simulated by the model, seeded)",
         "config": {"workload": args.workload},
-        "cpu_baseline": {"value": value, "unit": "particle-steps/s",
+        "cpu_baseline": {"value": value, "unit": unit,
                          "cores": threads, "kind": "port",
                          "sample": base["sample"]},
-        "e2e": {"value": value, "unit": "particle-steps/s",
+        "e2e": {"value": value, "unit": unit,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def serve_cpu_run(w, clients, threads):
+    """The first request of each listed client, one by one, on the CPU
+    oracle (the reference's engine restated; OpenMP over particles)."""
+    from oracle import pyoracle
+    import dust2_gb300 as d
+    port = pyoracle.port()
+    gen = d.Generator("seir_age")
+    total = 0
+    t0 = time.perf_counter()
+    for i in clients:
+        c = w["clients"][i]
+        n = c["n_particles"]
+        pars = gen.pack_pars(c["pars"][0])
+        data = np.asarray(c["data"]["incidence"], dtype=float)
+        rng = np.frombuffer(d.rng_streams(n + 2, c["seed"]), dtype="<u8")
+        port.filter_run("seir_age", pars, [n], 0.0, c["data"]["time"], data,
+                        1, w["dt"], rng, n_runs=1, n_state=96,
+                        n_threads=threads)
+        total += c["particle_steps"]
+    return time.perf_counter() - t0, total
+
+
+def serve_cpu_sample(w, target_seconds, threads):
+    """Clients (in order) whose first requests take about target_seconds
+    on the CPU."""
+    t, ps = serve_cpu_run(w, [0], threads)
+    rate = ps / max(t, 1e-9)
+    chosen, total = [0], ps
+    for i in range(1, len(w["clients"])):
+        if total / rate >= target_seconds:
+            break
+        chosen.append(i)
+        total += w["clients"][i]["particle_steps"]
+    base = {"sample": f"first requests of clients 1-{len(chosen)} of "
+                      f"{len(w['clients'])}, one by one"}
+    return chosen, base
 
 
 def oracle_simulate():
@@ -627,6 +860,9 @@ def main():
     elif args.workload == "serve_seir":
         if rank == 0:
             serve_arm(args, rank, world, local)
+    elif args.workload == "ode_batched":
+        if rank == 0:
+            ode_arm(args, rank, world, local)
     else:
         gpu_arm(args, rank, world, local)
 

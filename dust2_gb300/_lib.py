@@ -132,6 +132,10 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_int32]),
     "dust2_gb300_filter_kernel_times": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p, c_i64_p, c_double_p, c_i64_p]),
+    "dust2_gb300_system_simulate_device": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, ctypes.c_size_t, ctypes.c_void_p]),
+    "dust2_gb300_system_stream": (ctypes.c_int, [ctypes.c_void_p,
+                                                 c_void_pp]),
     "dust2_gb300_server_create": (ctypes.c_int, [
         ctypes.c_char_p, ctypes.c_double, ctypes.c_size_t, c_void_pp]),
     "dust2_gb300_server_free": (ctypes.c_int, [ctypes.c_void_p]),

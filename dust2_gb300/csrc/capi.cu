@@ -443,28 +443,53 @@ int dust2_gb300_system_run_to_time(dust2_gb300_system* sys, double time) {
   });
 }
 
+// r/system.hpp:286-327 (check_time_sequence of the output times)
+static void check_simulate_times(system_api& s, const double* times,
+                                 size_t n_times) {
+  check_errors(s, "simulate");
+  need(times != nullptr && n_times >= 1,
+       "Expected at least one value in 'times'");
+  if (times[0] < s.time()) {
+    char buf[200];
+    std::snprintf(buf, sizeof(buf),
+                  "Expected 'time[1]' (%d) to be larger than the previous "
+                  "value (%d)", static_cast<int>(times[0]),
+                  static_cast<int>(s.time()));
+    throw std::runtime_error(buf);
+  }
+  for (std::size_t i = 1; i < n_times; ++i) {
+    need(times[i] > times[i - 1], "Values in 'times' must be increasing");
+  }
+}
+
 int dust2_gb300_system_simulate(dust2_gb300_system* sys, const double* times,
                                 size_t n_times, const size_t* index_state,
                                 size_t n_index_state, double* out) {
   return guard([&] {
     auto& s = sysref(sys);
-    check_errors(s, "simulate");
-    need(n_times >= 1, "Expected at least one value in 'times'");
-    if (times[0] < s.time()) {
-      char buf[200];
-      std::snprintf(buf, sizeof(buf),
-                    "Expected 'time[1]' (%d) to be larger than the previous "
-                    "value (%d)", static_cast<int>(times[0]),
-                    static_cast<int>(s.time()));
-      throw std::runtime_error(buf);
-    }
-    for (std::size_t i = 1; i < n_times; ++i) {
-      need(times[i] > times[i - 1], "Values in 'times' must be increasing");
-    }
+    check_simulate_times(s, times, n_times);
     auto is = to_int_index(index_state, n_index_state, s.n_state(),
                            "index_state");
     s.simulate(times, static_cast<int>(n_times), is.empty() ? nullptr : is.data(),
                static_cast<int>(is.size()), out);
+  });
+}
+
+int dust2_gb300_system_simulate_device(dust2_gb300_system* sys,
+                                       const double* times, size_t n_times,
+                                       double* out_device) {
+  return guard([&] {
+    auto& s = sysref(sys);
+    check_simulate_times(s, times, n_times);
+    need(out_device != nullptr, "out_device is NULL");
+    s.simulate_device(times, static_cast<int>(n_times), out_device);
+  });
+}
+
+int dust2_gb300_system_stream(dust2_gb300_system* sys, void** stream) {
+  return guard([&] {
+    need(stream != nullptr, "stream is NULL");
+    *stream = sysref(sys).stream_handle();
   });
 }
 

@@ -37,6 +37,17 @@
 namespace dust2gpu {
 namespace random {
 
+// The two sampler cores are compiled once per kernel and called rather
+// than inlined at every draw site: a system drawing many binomials per
+// step (one per age class and transition) otherwise outgrows the
+// instruction cache, and the call costs only integer-pipe instructions on
+// an FP64-bound kernel.
+#if defined(__CUDACC__)
+#define DUST2_SAMPLER inline __host__ __device__ __noinline__
+#else
+#define DUST2_SAMPLER inline
+#endif
+
 // Bound on candidate draws in a rejection loop; with valid arguments the
 // acceptance rate is above 0.8, so reaching this means corrupt input.
 constexpr int MAX_REJECTION_ATTEMPTS = 100000;
@@ -53,7 +64,7 @@ constexpr int BINV_MAX_X = 110;
 // u stays >= 0 (it only loses a smaller r), so `u > r` is a bit compare.
 // The terms that depend on p only (q = 1 - p, s = p * rcp(q), log q) are
 // arguments, so that a prepared probability can supply them.
-DUST2_HD double binomial_inversion(rng_state& rng, double n, double p,
+DUST2_SAMPLER double binomial_inversion(rng_state& rng, double n, double p,
                                    double q, double s, double logq) {
   const double a = (n + 1.0) * s;
   const double r0 = math::exp(n * logq);  // q^n
@@ -96,7 +107,7 @@ struct btrs_lpq_ready {
 // reciprocals (math::rcp); us = 0 (u = -1/2 exactly) is rejected.  Here
 // n p >= 10 and q >= 1/2, so b > 6.8 and v_r > 0.3.
 template <typename LPQ>
-DUST2_HD double binomial_btrs(rng_state& rng, double n, double p, double q,
+DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
                               const LPQ& lpq_of) {
   const double spq = std::sqrt(n * p * q);
   const double b = 1.15 + 2.53 * spq;

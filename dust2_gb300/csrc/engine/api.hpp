@@ -85,6 +85,12 @@ public:
   virtual void simulate(const double* times, int n_times,
                         const int* index_state, int n_index_state,
                         double* out) = 0;
+  // simulate with all state, output left in device memory (out_dev, the
+  // same order); returns when the work is done
+  virtual void simulate_device(const double* times, int n_times,
+                               double* out_dev) = 0;
+  // the CUDA stream the system's work is issued on
+  virtual void* stream_handle() = 0;
   // index: group-local particle index per particle, group-major
   virtual void reorder(const int* index) = 0;
   // data: [group][n_data] doubles; out: [group][particle]

@@ -129,12 +129,18 @@ __global__ void k_ode_run(system_view<T> v, ode_view o,
   constexpr int NV = n_var_max<T>();
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
-  sm.load(v, tl.group);
+  const bool mixed = tl.group < 0;
+  if (!mixed) {
+    sm.load(v, tl.group);
+  }
   __syncthreads();
   if (static_cast<int>(threadIdx.x) >= tl.count) {
     return;
   }
   const int k = tl.start + threadIdx.x;
+  const int g = group_of(v, tl, k);
+  const auto& shared = mixed ? v.shared[g] : sm.shared();
+  const zero_every_spec& zero = mixed ? v.zero_every[g] : sm.zero;
   const int n_var = v.n_state - T::n_output;
   typename T::internal_state internal{};
   double y[T::n_state_max];
@@ -142,19 +148,19 @@ __global__ void k_ode_run(system_view<T> v, ode_view o,
   dopri5::state<NV> st;
   dopri5::scratch<NV> s;
   load_ode<NV>(o, k, n_var, st);
-  dopri5::solver<T, NV> sol{ctl, sm.shared(), internal, n_var, k};
-  if (requires_init[tl.group]) {
+  dopri5::solver<T, NV> sol{ctl, shared, internal, n_var, k};
+  if (requires_init[g]) {
     sol.initialise(time0, y, st, s);
   }
   double t = time0;
   for (int i = 0; i < n_times; ++i) {
     const double t_end = times[i];
     if (st.err == 0) {
-      sol.run(t, t_end, y, sm.zero, st, s);
+      sol.run(t, t_end, y, zero, st, s);
     }
     t = t_end;
     if (out != nullptr) {
-      refresh_output<T>(t_end, y, sm.shared(), internal);
+      refresh_output<T>(t_end, y, shared, internal);
       double* dst = out + (static_cast<long>(i) * n_total + k) * n_out;
       for (int j = 0; j < n_out; ++j) {
         const int sj = index_out == nullptr ? j : index_out[j];
@@ -167,7 +173,7 @@ __global__ void k_ode_run(system_view<T> v, ode_view o,
       }
     }
   }
-  refresh_output<T>(t, y, sm.shared(), internal);
+  refresh_output<T>(t, y, shared, internal);
   store_state<T>(v, k, y);
   store_ode<NV>(o, k, n_var, st);
   if (st.err != 0) {
@@ -182,16 +188,20 @@ template <typename T>
 __global__ void k_ode_output(system_view<T> v, double time) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
-  sm.load(v, tl.group);
+  const bool mixed = tl.group < 0;
+  if (!mixed) {
+    sm.load(v, tl.group);
+  }
   __syncthreads();
   if (static_cast<int>(threadIdx.x) >= tl.count) {
     return;
   }
   const int k = tl.start + threadIdx.x;
+  const auto& shared = mixed ? v.shared[group_of(v, tl, k)] : sm.shared();
   typename T::internal_state internal{};
   double y[T::n_state_max];
   load_state<T>(v, k, y);
-  refresh_output<T>(time, y, sm.shared(), internal);
+  refresh_output<T>(time, y, shared, internal);
   store_state<T>(v, k, y);
 }
 
@@ -348,11 +358,16 @@ public:
   }
 
   // Run through `times` leaving outputs in a caller-provided device
-  // buffer (used by benchmarks to keep outputs resident).
-  void simulate_device(const double* times, int n_times, double* out_dev) {
+  // buffer.
+  void simulate_device(const double* times, int n_times,
+                       double* out_dev) override {
     launch_run(times, n_times, out_dev, nullptr, base_.n_state());
     base_.check_errors_after();
     base_.set_time(times[n_times - 1]);
+  }
+
+  void* stream_handle() override {
+    return base_.stream_handle();
   }
 
   void reorder(const int* index) override {
@@ -498,8 +513,8 @@ private:
                                requires_initialise_.data(),
                                requires_initialise_.size() * sizeof(int),
                                cudaMemcpyHostToDevice, s));
-    k_ode_run<T><<<L.n_tiles(), L.tile_size, 0, s>>>(
-      base_.view(), view_ode(), control_dev(), base_.time(),
+    k_ode_run<T><<<base_.n_run_tiles(), L.tile_size, 0, s>>>(
+      base_.run_view(), view_ode(), control_dev(), base_.time(),
       times_dev_.data(), n_times, requires_init_dev_.data(), L.n_total,
       out_dev, index_dev, n_out);
     DUST2_CUDA(cudaGetLastError());
@@ -509,8 +524,8 @@ private:
   void refresh_outputs() {
     if constexpr (has_output<T>::value) {
       const auto& L = base_.layout();
-      k_ode_output<T><<<L.n_tiles(), L.tile_size, 0, base_.stream()>>>(
-        base_.view(), base_.time());
+      k_ode_output<T><<<base_.n_run_tiles(), L.tile_size, 0,
+                        base_.stream()>>>(base_.run_view(), base_.time());
       DUST2_CUDA(cudaGetLastError());
     }
   }

@@ -48,7 +48,16 @@ struct system_view {
   int stride;
   int n_state;
   bool deterministic;
+  const int* particle_group;     // [n_total], for packed tiles
 };
+
+// Group of particle k of tile tl (a packed tile's particles may belong to
+// different groups).
+template <typename T>
+__device__ __forceinline__ int group_of(const system_view<T>& v,
+                                        const tile& tl, int k) {
+  return tl.group >= 0 ? tl.group : v.particle_group[k];
+}
 
 // Steps of one launch whose zero_every test is precomputed per block.
 constexpr int ZERO_STEPS_CACHED = 64;
@@ -126,7 +135,7 @@ __device__ __forceinline__ void apply_zero_every(
     const zero_every_spec& z, const std::uint64_t* zero_steps, int step,
     double time, double* x) {
   for (int i = 0; i < z.n; ++i) {
-    const bool hit = step < ZERO_STEPS_CACHED ?
+    const bool hit = (zero_steps != nullptr && step < ZERO_STEPS_CACHED) ?
       ((zero_steps[i] >> step) & 1) != 0 : fmod(time, z.period[i]) == 0;
     if (hit) {
 #pragma unroll
@@ -188,23 +197,34 @@ struct min_blocks_of<T, std::void_t<decltype(T::min_blocks_per_sm)>> {
   __global__ void __launch_bounds__(default_tile_size<T>(),               \
                                     min_blocks_of<T>::value)
 
+// The per-particle kernels below run over a layout's run tiles: a block
+// whose particles share one group stages that group's shared state in
+// shared memory; in a packed tile each thread reads its own group's from
+// global memory.
 template <typename T>
 DUST2_PARTICLE_KERNEL(T) k_initial(system_view<T> v, const int* active,
                                    double time) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
-  sm.load(v, tl.group);
+  const bool mixed = tl.group < 0;
+  if (!mixed) {
+    sm.load(v, tl.group);
+  }
   __syncthreads();
-  if ((active != nullptr && !active[tl.group]) ||
-      static_cast<int>(threadIdx.x) >= tl.count) {
+  if (static_cast<int>(threadIdx.x) >= tl.count) {
     return;
   }
   const int k = tl.start + threadIdx.x;
+  const int g = group_of(v, tl, k);
+  if (active != nullptr && !active[g]) {
+    return;
+  }
+  const auto& shared = mixed ? v.shared[g] : sm.shared();
   auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
   typename T::internal_state internal{};
   double x[T::n_state_max];
   load_state<T>(v, k, x);
-  T::initial(time, sm.shared(), internal, rng, x);
+  T::initial(time, shared, internal, rng, x);
   store_state<T>(v, k, x);
   store_rng(v.rng, v.stride, k, rng);
   capture_error(v.errors, v.any_error, k, rng);
@@ -215,20 +235,26 @@ DUST2_PARTICLE_KERNEL(T) k_run(system_view<T> v, double time, double dt,
                                int n_steps) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
-  sm.load(v, tl.group);
-  sm.load_zero_steps(v, tl.group, time, dt, n_steps);
+  const bool mixed = tl.group < 0;
+  if (!mixed) {
+    sm.load(v, tl.group);
+    sm.load_zero_steps(v, tl.group, time, dt, n_steps);
+  }
   __syncthreads();
   if (static_cast<int>(threadIdx.x) >= tl.count) {
     return;
   }
   const int k = tl.start + threadIdx.x;
+  const int g = group_of(v, tl, k);
+  const auto& shared = mixed ? v.shared[g] : sm.shared();
+  const zero_every_spec& zero = mixed ? v.zero_every[g] : sm.zero;
   auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
   typename T::internal_state internal{};
   double x[T::n_state_max];
   double y[T::n_state_max];
   load_state<T>(v, k, x);
-  run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
-                  sm.zero_steps, rng, x, y);
+  run_particle<T>(time, dt, n_steps, shared, internal, zero,
+                  mixed ? nullptr : sm.zero_steps, rng, x, y);
   store_state<T>(v, k, x);
   store_rng(v.rng, v.stride, k, rng);
   capture_error(v.errors, v.any_error, k, rng);
@@ -242,19 +268,24 @@ DUST2_PARTICLE_KERNEL(T) k_compare(system_view<T> v, double time,
                           int n_groups_data, double* out) {
   __shared__ shared_smem<T> sm;
   const tile tl = v.tiles[blockIdx.x];
-  sm.load(v, tl.group);
+  const bool mixed = tl.group < 0;
+  if (!mixed) {
+    sm.load(v, tl.group);
+  }
   __syncthreads();
   if (static_cast<int>(threadIdx.x) >= tl.count) {
     return;
   }
   if constexpr (has_compare_data<T>::value) {
     const int k = tl.start + threadIdx.x;
+    const int g = group_of(v, tl, k);
+    const auto& shared = mixed ? v.shared[g] : sm.shared();
     auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
     typename T::internal_state internal{};
     double x[T::n_state_max];
     load_state<T>(v, k, x);
-    const auto& d = data[n_groups_data == 1 ? 0 : tl.group];
-    out[k] = T::compare_data(time, x, d, sm.shared(), internal, rng);
+    const auto& d = data[n_groups_data == 1 ? 0 : g];
+    out[k] = T::compare_data(time, x, d, shared, internal, rng);
     store_rng(v.rng, v.stride, k, rng);
     capture_error(v.errors, v.any_error, k, rng);
   }
@@ -306,6 +337,10 @@ public:
     shared_dev_.resize(shared_.size());
     zero_dev_.resize(shared_.size());
     tiles_.resize(layout_.tiles.size());
+    if (layout_.use_packed) {
+      packed_.resize(layout_.packed.size());
+      particle_group_.resize(layout_.n_total);
+    }
     offsets_dev_.resize(layout_.n_groups);
     errors_.resize(layout_.n_total);
     any_error_.resize(1);
@@ -321,6 +356,15 @@ public:
     DUST2_CUDA(cudaMemcpyAsync(zero_dev_.data(), z.data(),
                                z.size() * sizeof(zero_every_spec),
                                cudaMemcpyHostToDevice, stream_));
+    if (layout_.use_packed) {
+      DUST2_CUDA(cudaMemcpyAsync(packed_.data(), layout_.packed.data(),
+                                 layout_.packed.size() * sizeof(tile),
+                                 cudaMemcpyHostToDevice, stream_));
+      DUST2_CUDA(cudaMemcpyAsync(particle_group_.data(),
+                                 layout_.particle_group.data(),
+                                 layout_.n_total * sizeof(int),
+                                 cudaMemcpyHostToDevice, stream_));
+    }
     DUST2_CUDA(cudaMemcpyAsync(tiles_.data(), layout_.tiles.data(),
                                layout_.tiles.size() * sizeof(tile),
                                cudaMemcpyHostToDevice, stream_));
@@ -408,6 +452,20 @@ public:
   const int* group_offsets_dev() const {
     return offsets_dev_.data();
   }
+  // The view of the per-particle kernels (k_initial, k_run, k_compare and
+  // the ODE kernels): over the layout's run tiles.
+  system_view<T> run_view() {
+    system_view<T> v = view();
+    if (layout_.use_packed) {
+      v.tiles = packed_.data();
+      v.particle_group = particle_group_.data();
+    }
+    return v;
+  }
+  int n_run_tiles() const {
+    return static_cast<int>(layout_.run_tiles().size());
+  }
+
   const tile* tiles_dev() const {
     return tiles_.data();
   }
@@ -434,8 +492,8 @@ public:
   void launch_run(double t0, int n_steps) {
     if constexpr (has_update<T>::value) {
       if (n_steps > 0) {
-        k_run<T><<<layout_.n_tiles(), layout_.tile_size, 0, stream_>>>(
-          view(), t0, dt_, n_steps);
+        k_run<T><<<n_run_tiles(), layout_.tile_size, 0, stream_>>>(
+          run_view(), t0, dt_, n_steps);
         DUST2_CUDA(cudaGetLastError());
       }
     } else {
@@ -444,8 +502,8 @@ public:
   }
 
   void launch_initial(const int* active) {
-    k_initial<T><<<layout_.n_tiles(), layout_.tile_size, 0, stream_>>>(
-      view(), active, time_);
+    k_initial<T><<<n_run_tiles(), layout_.tile_size, 0, stream_>>>(
+      run_view(), active, time_);
     DUST2_CUDA(cudaGetLastError());
   }
 
@@ -554,6 +612,25 @@ public:
     check_errors_after();
   }
 
+  void simulate_device(const double* times, int n_times,
+                       double* out_dev) override {
+    const long per_time = static_cast<long>(layout_.n_total) * n_state_;
+    for (int i = 0; i < n_times; ++i) {
+      const int n_steps = n_steps_to(times[i]);
+      launch_run(time_, n_steps);
+      time_ = time_ + n_steps * dt_;
+      k_gather_state<<<n_blocks(per_time, 256), 256, 0, stream_>>>(
+        state_.data(), layout_.stride, layout_.n_total, nullptr, n_state_,
+        out_dev + static_cast<std::size_t>(i) * per_time);
+      DUST2_CUDA(cudaGetLastError());
+    }
+    check_errors_after();
+  }
+
+  void* stream_handle() override {
+    return static_cast<void*>(stream_);
+  }
+
   void reorder(const int* index) override {
     device_array<int> idx(layout_.n_total);
     DUST2_CUDA(cudaMemcpyAsync(idx.data(), index,
@@ -580,8 +657,8 @@ public:
       DUST2_CUDA(cudaMemcpyAsync(d_dev.data(), d.data(),
                                  d.size() * sizeof(data_type),
                                  cudaMemcpyHostToDevice, stream_));
-      k_compare<T><<<layout_.n_tiles(), layout_.tile_size, 0, stream_>>>(
-        view(), time_, d_dev.data(), n_groups_data, o.data());
+      k_compare<T><<<n_run_tiles(), layout_.tile_size, 0, stream_>>>(
+        run_view(), time_, d_dev.data(), n_groups_data, o.data());
       DUST2_CUDA(cudaGetLastError());
       DUST2_CUDA(cudaMemcpyAsync(out, o.data(),
                                  layout_.n_total * sizeof(double),
@@ -658,6 +735,8 @@ private:
   device_array<shared_state> shared_dev_;
   device_array<zero_every_spec> zero_dev_;
   device_array<tile> tiles_;
+  device_array<tile> packed_;
+  device_array<int> particle_group_;
   device_array<int> offsets_dev_;
   device_array<particle_error> errors_;
   device_array<int> any_error_;

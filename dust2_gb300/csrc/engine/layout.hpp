@@ -12,6 +12,7 @@
 // primitives.
 #pragma once
 
+#include <algorithm>
 #include <stdexcept>
 #include <vector>
 
@@ -19,10 +20,11 @@ namespace dust2gpu {
 namespace engine {
 
 struct tile {
-  int group;  // parameter group of every particle in the tile
+  int group;  // parameter group of every particle in the tile, or -1
+              // for a packed tile holding particles of several groups
   int start;  // global index of the first particle
   int count;  // particles in the tile (<= tile size)
-  int local;  // index of the first particle within its group
+  int local;  // index of the first particle within its group (-1 mixed)
 };
 
 struct group_layout {
@@ -31,6 +33,14 @@ struct group_layout {
   std::vector<int> tile_first;   // first tile of each group
   std::vector<int> tile_count;   // tiles in each group
   std::vector<tile> tiles;
+  // Packed tiles: consecutive runs of tile_size particles whatever their
+  // group, used by the per-particle kernels that need no reduction over a
+  // group when groups are small (many one-particle groups would otherwise
+  // leave one busy thread per block).  particle_group gives each
+  // particle's group.
+  std::vector<tile> packed;
+  std::vector<int> particle_group;
+  bool use_packed = false;
   int n_groups = 0;
   int n_total = 0;
   int stride = 0;                // SoA stride, a multiple of 32
@@ -72,6 +82,29 @@ struct group_layout {
     }
     n_total = static_cast<int>(total);
     stride = ((n_total + 31) / 32) * 32;
+    // smaller groups than a tile on average: pack them
+    use_packed = static_cast<long>(n_total) < static_cast<long>(n_groups) *
+      tile_size;
+    if (use_packed) {
+      particle_group.resize(n_total);
+      for (int g = 0; g < n_groups; ++g) {
+        std::fill(particle_group.begin() + offset[g],
+                  particle_group.begin() + offset[g] + n[g], g);
+      }
+      for (int start = 0; start < n_total; start += tile_size) {
+        const int count = std::min(tile_size, n_total - start);
+        const int g0 = particle_group[start];
+        const int g1 = particle_group[start + count - 1];
+        packed.push_back(g0 == g1 ?
+                         tile{g0, start, count, start - offset[g0]} :
+                         tile{-1, start, count, -1});
+      }
+    }
+  }
+
+  // The tiles of the per-particle kernels (packed when that helps).
+  const std::vector<tile>& run_tiles() const {
+    return use_packed ? packed : tiles;
   }
 
   int n_tiles() const {

@@ -188,7 +188,8 @@ __global__ void k_resample(filter_view f) {
   // total differs by at most (n + L + 10) u uu.  So a decision is safe
   // when the prefix is farther than (k + n + 2L + 16) u max(S_k, uu)
   // from the target (5% slack on top).
-  const double L = 2.0 + ceil(log2(static_cast<double>(n)));
+  // ceil(log2 n) on the integer pipe
+  const double L = 2.0 + (n > 1 ? 32 - __clz(n - 1) : 0);
   const double eps = 0x1.0p-53 * 1.05;
   bool ok = true;
   if (m > 0) {

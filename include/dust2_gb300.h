@@ -164,6 +164,18 @@ int dust2_gb300_system_simulate(dust2_gb300_system* sys, const double* times,
                                 size_t n_times, const size_t* index_state,
                                 size_t n_index_state, double* out);
 
+/* As dust2_gb300_system_simulate with all state, writing into device
+ * memory at out_device (n_times * n_particles * n_groups * n_state
+ * doubles, the same order); returns when done.  No counterpart in dust2,
+ * whose verb returns host arrays: for callers that keep results on the
+ * GPU. */
+int dust2_gb300_system_simulate_device(dust2_gb300_system* sys,
+                                       const double* times, size_t n_times,
+                                       double* out_device);
+
+/* The CUDA stream (cudaStream_t) the system's work is issued on. */
+int dust2_gb300_system_stream(dust2_gb300_system* sys, void** stream);
+
 /* dust2_system_reorder (r/system.hpp:199-221): index has
  * n_particles * n_groups entries, each a particle index within its group. */
 int dust2_gb300_system_reorder(dust2_gb300_system* sys, const size_t* index,
