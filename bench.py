@@ -149,6 +149,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x, world, device):
+    """The largest value of x over the ranks (the slowest replica's time);
+    x itself on one rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds_max):
+    """Units processed by all replicas per second of the slowest one."""
+    return units_per_rank * world / seconds_max
+
+
 def fp64_peak_tflops():
     """DFMA throughput microbenchmark (FP64 FMA chains, all SMs)."""
     import ctypes
@@ -336,12 +353,8 @@ def gpu_arm(args, rank, world, local):
         ctypes.byref(n_run)))
     _lib.check(lib.dust2_gb300_filter_set_timing(h, 0))
     ms = float(np.mean(elapsed))
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = particle_steps * world / (ms_max * 1e-3)
+    ms_max = max_over_ranks(ms, world, "cuda")
+    value = whole_job_rate(particle_steps, world, ms_max * 1e-3)
 
     # end to end through the public API: host parameters in, host
     # log-likelihoods out, every step
@@ -353,11 +366,7 @@ def gpu_arm(args, rank, world, local):
         e2e_times.append(time.perf_counter() - t0)
     assert np.all(np.isfinite(res))
     e2e_s = float(np.mean(e2e_times))
-    e2e_max = e2e_s
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_max = float(t.item())
+    e2e_max = max_over_ranks(e2e_s, world, "cuda")
     h2d = n_groups * gen.n_pars * 8
     d2h = n_groups * 8 + n_groups * 4 + 4
 

@@ -4,7 +4,8 @@ csrc/ (C ABI: include/dust2_gb300.h)."""
 
 from ._lib import DustError, device_count
 from .interface import (
-    DustLikelihood, DustServer, DustSystem, Generator, dust_filter_create,
+    DustLikelihood, DustServer, DustSystem, DustUnfilter, Generator,
+    dust_filter_create,
     dust_filter_data, dust_likelihood_last_state, dust_likelihood_rng_state,
     dust_likelihood_run, dust_likelihood_serial_fallbacks,
     dust_likelihood_server, dust_likelihood_set_rng_state, dust_ode_control,
@@ -13,11 +14,13 @@ from .interface import (
     dust_system_set_rng_state, dust_system_set_state,
     dust_system_set_state_initial, dust_system_set_time,
     dust_system_simulate, dust_system_state, dust_system_time,
-    dust_system_update_pars, logistic, resample_weight, rng_streams,
+    dust_system_update_pars, dust_unfilter_create, logistic,
+    resample_weight, rng_streams,
     scale_log_weights, seir_age, sir, sir_cases, sirode, walk)
 
 __all__ = [
-    "DustError", "DustLikelihood", "DustServer", "DustSystem", "Generator",
+    "DustError", "DustLikelihood", "DustServer", "DustSystem",
+    "DustUnfilter", "Generator",
     "device_count", "dust_filter_create", "dust_filter_data",
     "dust_likelihood_last_state", "dust_likelihood_rng_state",
     "dust_likelihood_run", "dust_likelihood_serial_fallbacks",
@@ -28,6 +31,7 @@ __all__ = [
     "dust_system_run_to_time", "dust_system_set_rng_state",
     "dust_system_set_state", "dust_system_set_state_initial",
     "dust_system_set_time", "dust_system_simulate", "dust_system_state",
-    "dust_system_time", "dust_system_update_pars", "logistic",
+    "dust_system_time", "dust_system_update_pars", "dust_unfilter_create",
+    "logistic",
     "resample_weight", "rng_streams", "scale_log_weights", "seir_age", "sir",
     "sir_cases", "sirode", "walk"]

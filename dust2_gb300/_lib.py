@@ -136,6 +136,20 @@ _SIGNATURES = {
         ctypes.c_void_p, c_double_p, ctypes.c_size_t, ctypes.c_void_p]),
     "dust2_gb300_system_stream": (ctypes.c_int, [ctypes.c_void_p,
                                                  c_void_pp]),
+    "dust2_gb300_unfilter_alloc": (ctypes.c_int, [
+        ctypes.c_char_p, c_double_p, ctypes.c_size_t, ctypes.c_size_t,
+        ctypes.c_double, c_double_p, ctypes.c_size_t, c_double_p,
+        ctypes.c_size_t, ctypes.c_double, ctypes.POINTER(OdeControl),
+        c_void_pp]),
+    "dust2_gb300_unfilter_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "dust2_gb300_unfilter_run": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, c_size_p, ctypes.c_size_t, c_double_p]),
+    "dust2_gb300_unfilter_update_pars": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, c_size_p, ctypes.c_size_t]),
+    "dust2_gb300_unfilter_state": (ctypes.c_int, [ctypes.c_void_p,
+                                                  c_double_p]),
+    "dust2_gb300_unfilter_dim": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, c_size_p, c_size_p, c_size_p]),
     "dust2_gb300_server_create": (ctypes.c_int, [
         ctypes.c_char_p, ctypes.c_double, ctypes.c_size_t, c_void_pp]),
     "dust2_gb300_server_free": (ctypes.c_int, [ctypes.c_void_p]),

@@ -35,6 +35,10 @@ struct dust2_gb300_server {
   std::unique_ptr<dust2gpu::engine::server_api> impl;
 };
 
+struct dust2_gb300_unfilter {
+  std::unique_ptr<dust2gpu::engine::unfilter_api> impl;
+};
+
 namespace dust2gpu {
 namespace engine {
 
@@ -192,6 +196,11 @@ system_api& sysref(dust2_gb300_system* sys) {
 filter_api& filref(dust2_gb300_filter* f) {
   need(f != nullptr && f->impl != nullptr, "Invalid filter handle");
   return *f->impl;
+}
+
+dust2gpu::engine::unfilter_api& unfref(dust2_gb300_unfilter* u) {
+  need(u != nullptr && u->impl != nullptr, "Invalid unfilter handle");
+  return *u->impl;
 }
 
 dust2gpu::engine::server_api& servref(dust2_gb300_server* s) {
@@ -794,6 +803,87 @@ int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
     filref(filter).kernel_times(step_ms, &a, run_ms, &b);
     *n_step_launches = a;
     *n_runs = b;
+  });
+}
+
+int dust2_gb300_unfilter_alloc(const char* name, const double* pars,
+                               size_t n_groups, size_t n_particles,
+                               double time_start, const double* time,
+                               size_t n_time, const double* data,
+                               size_t n_groups_data, double dt,
+                               const dust2_gb300_ode_control* control,
+                               dust2_gb300_unfilter** out) {
+  return guard([&] {
+    need(out != nullptr && pars != nullptr && data != nullptr,
+         "NULL argument");
+    need(n_groups >= 1, "'n_groups' must be at least 1");
+    need(n_particles >= 1, "'n_particles' must be at least 1");
+    need(n_groups_data == 1 || n_groups_data == n_groups,
+         "Expected 'data' to have 1 or n_groups groups");
+    check_data_times(time_start, time, n_time);
+    const auto* f = dust2gpu::engine::find_system(name);
+    need(f->continuous || dt > 0, "Expected 'dt' to be greater than 0");
+    std::vector<int> np(n_groups, static_cast<int>(n_particles));
+    auto* impl = f->create_unfilter(pars, static_cast<int>(n_groups), np,
+                                    time_start, time,
+                                    static_cast<int>(n_time), data,
+                                    static_cast<int>(n_groups_data), dt,
+                                    to_control(control));
+    *out = new dust2_gb300_unfilter{
+      std::unique_ptr<dust2gpu::engine::unfilter_api>(impl)};
+  });
+}
+
+int dust2_gb300_unfilter_free(dust2_gb300_unfilter* unfilter) {
+  return guard([&] { delete unfilter; });
+}
+
+int dust2_gb300_unfilter_run(dust2_gb300_unfilter* unfilter,
+                             const double* initial,
+                             const size_t* index_group,
+                             size_t n_index_group, double* ll) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(ll != nullptr, "ll is NULL");
+    auto ig = to_int_index(index_group, n_index_group, u.sys().n_groups(),
+                           "index_group");
+    u.run(initial, ig.empty() ? nullptr : ig.data(),
+          static_cast<int>(ig.size()), ll);
+  });
+}
+
+int dust2_gb300_unfilter_update_pars(dust2_gb300_unfilter* unfilter,
+                                     const double* pars,
+                                     const size_t* index_group,
+                                     size_t n_index_group) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(pars != nullptr, "pars is NULL");
+    auto ig = to_int_index(index_group, n_index_group, u.sys().n_groups(),
+                           "index_group");
+    u.update_pars(pars, ig.empty() ? nullptr : ig.data(),
+                  static_cast<int>(ig.size()));
+  });
+}
+
+int dust2_gb300_unfilter_dim(const dust2_gb300_unfilter* unfilter,
+                             size_t* n_state, size_t* n_particles_total,
+                             size_t* n_groups, size_t* n_time) {
+  return guard([&] {
+    need(unfilter != nullptr && unfilter->impl != nullptr,
+         "Invalid unfilter handle");
+    auto& u = *unfilter->impl;
+    *n_state = u.sys().n_state();
+    *n_particles_total = u.sys().n_particles_total();
+    *n_groups = u.sys().n_groups();
+    *n_time = u.n_times();
+  });
+}
+
+int dust2_gb300_unfilter_state(dust2_gb300_unfilter* unfilter, double* out) {
+  return guard([&] {
+    need(out != nullptr, "out is NULL");
+    unfref(unfilter).sys().get_state(out);
   });
 }
 

@@ -142,5 +142,20 @@ public:
                             double* run_ms, long* n_runs) = 0;
 };
 
+// The deterministic likelihood (dust2::unfilter, unfilter.hpp:10-73).
+class unfilter_api {
+public:
+  virtual ~unfilter_api() = default;
+  virtual system_api& sys() = 0;
+  virtual int n_times() const = 0;
+  // initial: optional full state used instead of the initial conditions;
+  // index_group: groups to run (nullptr = all); ll_out: n_particles
+  // values per requested group, in index_group order.
+  virtual void run(const double* initial, const int* index_group,
+                   int n_index_group, double* ll_out) = 0;
+  virtual void update_pars(const double* pars, const int* index_group,
+                           int n_index_group) = 0;
+};
+
 }  // namespace engine
 }  // namespace dust2gpu

@@ -337,6 +337,30 @@ public:
     }
   }
 
+  discrete_system<T>& base() {
+    return base_;
+  }
+
+  // Launch a whole-run kernel of the unfilter (engine/unfilter.cuh) with
+  // this system's solver record: kernel(view, ode view, control, time,
+  // times, n_times, requires_init, active, data, n_groups_data, ll).
+  template <typename K, typename D>
+  void launch_unfilter(const double* times_dev, int n_times,
+                       const int* active, const D* data, int n_groups_data,
+                       double* ll, K kernel) {
+    const auto& L = base_.layout();
+    auto s = base_.stream();
+    DUST2_CUDA(cudaMemcpyAsync(requires_init_dev_.data(),
+                               requires_initialise_.data(),
+                               requires_initialise_.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    kernel<<<base_.n_run_tiles(), L.tile_size, 0, s>>>(
+      base_.run_view(), view_ode(), control_dev(), base_.time(), times_dev,
+      n_times, requires_init_dev_.data(), active, data, n_groups_data, ll);
+    DUST2_CUDA(cudaGetLastError());
+    std::fill(requires_initialise_.begin(), requires_initialise_.end(), 0);
+  }
+
   void simulate(const double* times, int n_times, const int* index_state,
                 int n_index_state, double* out) override {
     const auto& L = base_.layout();

@@ -15,6 +15,7 @@
 #include "lf_table.hpp"
 #include "registry.hpp"
 #include "served.cuh"
+#include "unfilter.cuh"
 
 namespace dust2gpu {
 namespace engine {
@@ -113,6 +114,48 @@ server_api* create_server(double hbm_budget_bytes, int max_sessions) {
   }
 }
 
+// r/discrete/unfilter.hpp:14-56, r/continuous/unfilter.hpp:14-56: a
+// deterministic system (the streams of seed 42, never advanced).
+template <typename T>
+unfilter_api* create_unfilter(const double* pars, int n_groups,
+                              const std::vector<int>& n_particles,
+                              double time_start, const double* times,
+                              int n_times, const double* data,
+                              int n_groups_data, double dt,
+                              const ode_control& control) {
+  if constexpr (!has_compare_data<T>::value) {
+    throw std::runtime_error(
+      std::string("Can't create unfilter; the '") + T::name +
+      "' system does not have 'compare_data' support");
+  } else {
+    bind_lf_table();
+    auto shared = build_shared_groups<T>(pars, n_groups);
+    long n_total = 0;
+    for (int n : n_particles) {
+      n_total += n;
+    }
+    const auto words = make_streams_from_seed(42, n_total);
+    std::vector<typename T::data_type> d;
+    const int nd = static_cast<int>(sizeof(typename T::data_type) /
+                                    sizeof(double));
+    for (int i = 0; i < n_times * n_groups_data; ++i) {
+      d.push_back(T::build_data(data + static_cast<std::size_t>(i) * nd));
+    }
+    std::vector<double> t(times, times + n_times);
+    if constexpr (is_continuous<T>()) {
+      auto sys = std::make_unique<continuous_system<T>>(
+        std::move(shared), time_start, control, n_particles, words, true);
+      return new unfilter_engine<T>(std::move(sys), time_start, std::move(t),
+                                    std::move(d), n_groups_data);
+    } else {
+      auto sys = std::make_unique<discrete_system<T>>(
+        std::move(shared), time_start, dt, n_particles, words, true);
+      return new unfilter_engine<T>(std::move(sys), time_start, std::move(t),
+                                    std::move(d), n_groups_data);
+    }
+  }
+}
+
 template <typename T>
 struct registrar {
   system_factory factory;
@@ -124,6 +167,7 @@ struct registrar {
     factory.create_system = &create_system<T>;
     factory.create_filter = &create_filter<T>;
     factory.create_server = &create_server<T>;
+    factory.create_unfilter = &create_unfilter<T>;
     register_system(&factory);
   }
 };

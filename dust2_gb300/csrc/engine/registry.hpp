@@ -38,6 +38,12 @@ struct system_factory {
                                int tile_size);
   // nullptr for systems without a filter (continuous time, no compare).
   server_api* (*create_server)(double hbm_budget_bytes, int max_sessions);
+  unfilter_api* (*create_unfilter)(const double* pars, int n_groups,
+                                   const std::vector<int>& n_particles,
+                                   double time_start, const double* times,
+                                   int n_times, const double* data,
+                                   int n_groups_data, double dt,
+                                   const ode_control& control);
 };
 
 void register_system(const system_factory* f);

@@ -826,8 +826,99 @@ def dust_filter_create(generator, time_start, data, n_particles,
                           npg if uneven else None)
 
 
+class DustUnfilter:
+    """A deterministic likelihood (the `dust_unfilter` object)."""
+
+    def __init__(self, generator, time_start, data, n_particles, n_groups,
+                 dt, ode_control, preserve_particle_dimension,
+                 preserve_group_dimension):
+        self.generator = generator
+        self.time_start = time_start
+        self.data = data
+        self.n_particles = n_particles
+        self.n_particles_per_group = None
+        self.n_groups = n_groups
+        self.dt = dt
+        self.ode_control = ode_control
+        self.preserve_particle_dimension = preserve_particle_dimension
+        self.preserve_group_dimension = preserve_group_dimension
+        self.deterministic = True
+        self._handle = None
+        self.n_state = None
+
+    @property
+    def ptr(self):
+        return self._handle
+
+    def initialise(self, pars):
+        flat = as_f64(np.concatenate([self.generator.pack_pars(p)
+                                      for p in pars]))
+        rows = as_f64(self.data["rows"])
+        times = as_f64(self.data["time"])
+        ctl = None
+        keep = None
+        if self.generator.time_type == "continuous":
+            c = self.ode_control if self.ode_control is not None else \
+                dust_ode_control()
+            ctl, keep = _ode_control_struct(c)
+        handle = ctypes.c_void_p()
+        check(_lib.lib().dust2_gb300_unfilter_alloc(
+            self.generator.name.encode(), dptr(flat), self.n_groups,
+            self.n_particles, self.time_start, dptr(times), times.size,
+            dptr(rows), self.data["n_groups_data"],
+            self.dt if self.dt is not None else 0.0,
+            None if ctl is None else ctypes.byref(ctl),
+            ctypes.byref(handle)))
+        del keep
+        self._handle = handle
+        n_state = ctypes.c_size_t()
+        n_tot = ctypes.c_size_t()
+        n_g = ctypes.c_size_t()
+        n_t = ctypes.c_size_t()
+        check(_lib.lib().dust2_gb300_unfilter_dim(
+            handle, ctypes.byref(n_state), ctypes.byref(n_tot),
+            ctypes.byref(n_g), ctypes.byref(n_t)))
+        self.n_state = n_state.value
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.dust2_gb300_unfilter_free(h)
+            self._handle = None
+
+
+def dust_unfilter_create(generator, time_start, data, n_particles=1,
+                         n_groups=None, dt=None, ode_control=None,
+                         shared_data=False, n_threads=1,
+                         preserve_particle_dimension=False,
+                         preserve_group_dimension=False):
+    """R/interface-unfilter.R:20-70."""
+    gen = _generator(generator)
+    if not gen.has_compare:
+        raise DustError(f"Can't create unfilter; the '{gen.name}' system "
+                        "does not have 'compare_data' support")
+    n_particles = _scalar_size(n_particles, "n_particles")
+    d = _prepare_data(data, n_groups, shared_data, gen)
+    time_start = float(time_start)
+    if time_start > d["time"][0]:
+        raise DustError(f"'time_start' ({time_start:g}) is later than the "
+                        f"first time in 'data' ({d['time'][0]:g})")
+    if gen.time_type == "discrete":
+        if ode_control is not None:
+            raise DustError(
+                "Can't use 'ode_control' with discrete-time systems")
+        dt = _check_dt(dt, gen)
+    elif dt is not None:
+        raise DustError("Can't use 'dt' with continuous-time systems")
+    n_groups = d["n_groups"]
+    return DustUnfilter(gen, time_start, d, n_particles, n_groups, dt,
+                        ode_control,
+                        preserve_particle_dimension or n_particles > 1,
+                        preserve_group_dimension or n_groups > 1)
+
+
 def _check_lik(obj):
-    if not isinstance(obj, DustLikelihood):
+    if not isinstance(obj, (DustLikelihood, DustUnfilter)):
         raise DustError("Expected 'obj' to be a 'dust_likelihood' object")
 
 
@@ -853,8 +944,11 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
     elif pars is not None:
         flat = as_f64(np.concatenate([obj.generator.pack_pars(p)
                                       for p in pars]))
-        check(_lib.lib().dust2_gb300_filter_update_pars(
-            obj.ptr, dptr(flat), sptr(ig), 0 if ig is None else ig.size))
+        update = (_lib.lib().dust2_gb300_unfilter_update_pars
+                  if isinstance(obj, DustUnfilter) else
+                  _lib.lib().dust2_gb300_filter_update_pars)
+        check(update(obj.ptr, dptr(flat), sptr(ig),
+                     0 if ig is None else ig.size))
     init = None
     if initial is not None:
         if obj.n_particles_per_group is not None:
@@ -870,6 +964,20 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
                                       obj.n_groups))
         init = as_f64(full.transpose(2, 1, 0))
     n_out = obj.n_groups if ig is None else ig.size
+    if isinstance(obj, DustUnfilter):
+        # r/unfilter.hpp:48-61: n_particles values per group
+        ll = np.empty(n_out * obj.n_particles)
+        check(_lib.lib().dust2_gb300_unfilter_run(
+            obj.ptr, dptr(init), sptr(ig), 0 if ig is None else ig.size,
+            dptr(ll)))
+        ll = ll.reshape(n_out, obj.n_particles).T
+        if obj.preserve_particle_dimension and obj.preserve_group_dimension:
+            return ll
+        if obj.preserve_particle_dimension:
+            return ll[:, 0]
+        if obj.preserve_group_dimension:
+            return ll[0, :]
+        return float(ll[0, 0])
     ll = np.empty(n_out)
     check(_lib.lib().dust2_gb300_filter_run(
         obj.ptr, dptr(init), sptr(ig), 0 if ig is None else ig.size,

@@ -330,6 +330,50 @@ int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
                                     double* step_ms, int64_t* n_step_launches,
                                     double* run_ms, int64_t* n_runs);
 
+/* ---- deterministic likelihood (r/unfilter.hpp, unfilter.hpp) ---------- */
+
+typedef struct dust2_gb300_unfilter dust2_gb300_unfilter;
+
+/* dust2_unfilter_<sys>_alloc (r/discrete/unfilter.hpp:14-56,
+ * r/continuous/unfilter.hpp:14-56): a deterministic system of n_groups x
+ * n_particles with data as for dust2_gb300_filter_alloc; control (may be
+ * NULL for the defaults) applies to continuous-time systems, dt to
+ * discrete-time ones. */
+int dust2_gb300_unfilter_alloc(const char* name, const double* pars,
+                               size_t n_groups, size_t n_particles,
+                               double time_start, const double* time,
+                               size_t n_time, const double* data,
+                               size_t n_groups_data, double dt,
+                               const dust2_gb300_ode_control* control,
+                               dust2_gb300_unfilter** out);
+
+int dust2_gb300_unfilter_free(dust2_gb300_unfilter* unfilter);
+
+/* dust2_unfilter_<sys>_run (r/unfilter.hpp:20-62, unfilter.hpp:42-73):
+ * initial (NULL = initial conditions) is a full state in dust2's order;
+ * ll receives n_particles values per group of index_group (NULL = all),
+ * the log-likelihood of each particle summed over the data. */
+int dust2_gb300_unfilter_run(dust2_gb300_unfilter* unfilter,
+                             const double* initial,
+                             const size_t* index_group,
+                             size_t n_index_group, double* ll);
+
+/* dust2_unfilter_<sys>_update_pars (r/unfilter.hpp:10-18). */
+int dust2_gb300_unfilter_update_pars(dust2_gb300_unfilter* unfilter,
+                                     const double* pars,
+                                     const size_t* index_group,
+                                     size_t n_index_group);
+
+/* Dimensions: state length, particles over all groups, groups, data
+ * times. */
+int dust2_gb300_unfilter_dim(const dust2_gb300_unfilter* unfilter,
+                             size_t* n_state, size_t* n_particles_total,
+                             size_t* n_groups, size_t* n_time);
+
+/* State after the last run (dust_likelihood_last_state for an unfilter):
+ * n_state x n_particles x n_groups doubles. */
+int dust2_gb300_unfilter_state(dust2_gb300_unfilter* unfilter, double* out);
+
 /* ---- likelihood server ---------------------------------------------------
  *
  * Continuous batching of filter likelihoods for many concurrent callers

@@ -889,6 +889,121 @@ int oracle_filter_run(const char* name, const double* pars, int n_groups,
   }
 }
 
+// dust2::unfilter (unfilter.hpp:42-73, reset :162-186) on a deterministic
+// system: initial conditions, then for each data time run_to_time and
+// compare_data, summing per particle.  ll_out: [n_runs][group][particle];
+// state_out (optional): the state after the last run.
+int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
+                        int n_particles, double time_start,
+                        const double* times, int n_times, const double* data,
+                        int n_groups_data, double dt, int max_steps,
+                        double atol, double rtol, double step_size_min,
+                        double step_size_max, int n_runs, double* ll_out,
+                        double* state_out, int n_threads, char* err,
+                        int err_len) {
+  try {
+    const size_t n_total = static_cast<size_t>(n_groups) * n_particles;
+    const std::string nm(name);
+    if (nm == "sirode") {
+      using S = dust2gpu::systems::sirode;
+      auto shared = shared_of<S>(pars, n_groups);
+      const int n_state = S::n_state(shared[0]);
+      const int n_var = n_state - S::n_output;
+      ode_ctl ctl;
+      ctl.max_steps = max_steps;
+      ctl.atol = atol;
+      ctl.rtol = rtol;
+      ctl.step_size_min = step_size_min;
+      ctl.step_size_max = step_size_max;
+      std::vector<typename S::data_type> d;
+      for (int i = 0; i < n_times * n_groups_data; ++i) {
+        d.push_back(S::build_data(data + i));
+      }
+      for (int r = 0; r < n_runs; ++r) {
+        errors err_k(n_total);
+#pragma omp parallel for schedule(static) num_threads(n_threads)
+        for (long k = 0; k < static_cast<long>(n_total); ++k) {
+          const int g = k / n_particles;
+          typename S::internal_state internal{};
+          rng_t rng{};
+          rng.deterministic = true;
+          std::vector<double> y(n_state, 0.0);
+          S::initial(time_start, shared[g], internal, rng, y.data());
+          ode_internals in(n_var);
+          dopri5_port<S> sol(ctl, shared[g], n_var);
+          const auto z = zero_every_of<S>(shared[g]);
+          double acc = 0;
+          try {
+            sol.initialise(time_start, y.data(), in);
+            double t = time_start;
+            for (int i = 0; i < n_times; ++i) {
+              sol.run(t, times[i], y.data(), z, in);
+              t = times[i];
+              acc += S::compare_data(
+                t, y.data(), d[i * n_groups_data + (n_groups_data == 1 ? 0 :
+                                                    g)],
+                shared[g], internal, rng);
+            }
+          } catch (const std::exception& e) {
+            err_k.e[k].code = std::string(e.what()) == "too many steps" ?
+              dust2gpu::ERR_ODE_TOO_MANY_STEPS :
+              dust2gpu::ERR_ODE_STEP_TOO_SMALL;
+          }
+          ll_out[r * n_total + k] = acc;
+          if (state_out != nullptr && r == n_runs - 1) {
+            std::copy(y.begin(), y.end(), state_out + k * n_state);
+          }
+        }
+        err_k.report();
+      }
+      return 0;
+    }
+    bool ok = dispatch_discrete(name, [&](auto t) {
+      using S = typename decltype(t)::type;
+      if constexpr (dust2gpu::has_compare_data<S>::value) {
+        std::vector<int> np(n_groups, n_particles);
+        std::vector<uint64_t> words(4 * n_total, 0);
+        discrete_sys<S> sys(shared_of<S>(pars, n_groups), np, time_start, dt,
+                            words.data(), true, n_threads);
+        std::vector<typename S::data_type> d;
+        const int nd = sizeof(typename S::data_type) / sizeof(double);
+        for (int i = 0; i < n_times * n_groups_data; ++i) {
+          d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+        }
+        const std::vector<char> active(n_groups, 1);
+        std::vector<double> step(n_total);
+        for (int r = 0; r < n_runs; ++r) {
+          sys.time = time_start;
+          sys.set_state_initial();
+          double* ll = ll_out + static_cast<size_t>(r) * n_total;
+          std::fill(ll, ll + n_total, 0.0);
+          for (int i = 0; i < n_times; ++i) {
+            sys.run_to_time(times[i], active);
+            sys.compare_data(d.data() + static_cast<size_t>(i) *
+                             n_groups_data, n_groups_data, active,
+                             step.data());
+            for (size_t k = 0; k < n_total; ++k) {
+              ll[k] += step[k];
+            }
+          }
+        }
+        if (state_out != nullptr) {
+          std::copy(sys.state.begin(), sys.state.end(), state_out);
+        }
+      } else {
+        throw std::runtime_error("system has no compare_data");
+      }
+    });
+    if (!ok) {
+      throw std::runtime_error("unknown system " + nm);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
 int oracle_ode_simulate(const char* name, const double* pars, int n_groups,
                         int n_particles, double time, int max_steps,
                         double atol, double rtol, double step_size_min,

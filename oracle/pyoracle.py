@@ -47,6 +47,7 @@ class Oracle:
         self._cmp = getattr(lib, p + "compare")
         self._flt = getattr(lib, p + "filter_run")
         self._ode = getattr(lib, p + "ode_simulate")
+        self._unf = getattr(lib, p + "unfilter_run")
         self._slw = getattr(lib, p + "scale_log_weights")
         self._slw.restype = ctypes.c_double
         self._slw.argtypes = [_n, _d]
@@ -161,6 +162,31 @@ class Oracle:
             args.append(_n(n_threads))
         self._call(self._ode, *args)
         return out, stats.reshape(n_total, 3)
+
+    def unfilter_run(self, name, pars, n_groups, n_particles, time_start,
+                     times, data, n_groups_data, n_state, dt=1.0,
+                     max_steps=10000, atol=1e-6, rtol=1e-6,
+                     step_size_min=np.finfo(float).eps,
+                     step_size_max=np.inf, n_runs=1, n_threads=1):
+        """Deterministic likelihood runs (dust2::unfilter); returns
+        (ll [n_runs][group][particle], state after the last run)."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        n_total = n_groups * n_particles
+        ll = np.empty(n_runs * n_total)
+        state = np.empty(n_total * n_state)
+        args = [_c(name.encode()), _dp(pars), _n(n_groups), _n(n_particles),
+                ctypes.c_double(time_start), _dp(times), _n(times.size),
+                _dp(data), _n(n_groups_data), ctypes.c_double(dt),
+                _n(max_steps), ctypes.c_double(atol), ctypes.c_double(rtol),
+                ctypes.c_double(step_size_min),
+                ctypes.c_double(step_size_max), _n(n_runs), _dp(ll),
+                _dp(state)]
+        if self.kind == "port":
+            args.append(_n(n_threads))
+        self._call(self._unf, *args)
+        return ll.reshape(n_runs, n_groups, n_particles), state
 
     def scale_log_weights(self, w):
         w = np.array(w, dtype=np.float64)

@@ -23,6 +23,7 @@
 #include <dust2/discrete/system.hpp>
 #include <dust2/filter.hpp>
 #include <dust2/filter_details.hpp>
+#include <dust2/unfilter.hpp>
 
 #include "engine/error_text.hpp"
 #include "systems/logistic.hpp"
@@ -408,6 +409,79 @@ int ref_ode_simulate(const char* name, const double* pars, int n_groups,
     } else if (nm == "logistic") {
       body(tag<ref_logistic>{}, tag<dust2gpu::systems::logistic>{});
     } else {
+      throw std::runtime_error("unknown system " + nm);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// dust2::unfilter (unfilter.hpp:42-73) on a deterministic system seeded
+// 42, as r/discrete/unfilter.hpp and r/continuous/unfilter.hpp build it;
+// n_runs runs at the same parameters.  ll_out: [n_runs][group][particle];
+// state_out: the state after the last run.
+int ref_unfilter_run(const char* name, const double* pars, int n_groups,
+                     int n_particles, double time_start, const double* times,
+                     int n_times, const double* data, int n_groups_data,
+                     double dt, int max_steps, double atol, double rtol,
+                     double step_size_min, double step_size_max, int n_runs,
+                     double* ll_out, double* state_out, char* err,
+                     int err_len) {
+  try {
+    std::vector<double> tt(times, times + n_times);
+    std::vector<uint64_t> seed{42};
+    auto finish = [&](auto& obj) {
+      for (int r = 0; r < n_runs; ++r) {
+        obj.run(true, false, {}, {}, obj.sys.all_groups());
+        const auto& ll = obj.last_log_likelihood();
+        std::copy(ll.begin(), ll.end(),
+                  ll_out + static_cast<size_t>(r) * n_groups * n_particles);
+      }
+      const auto& st = obj.sys.state();
+      std::copy(st.begin(), st.end(), state_out);
+    };
+    auto data_of = [&](auto s) {
+      using S = typename decltype(s)::type;
+      std::vector<typename S::data_type> d;
+      const int nd = sizeof(typename S::data_type) / sizeof(double);
+      for (int i = 0; i < n_times * n_groups_data; ++i) {
+        d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+      }
+      return d;
+    };
+    const std::string nm(name);
+    if (nm == "sirode") {
+      using S = dust2gpu::systems::sirode;
+      using T = ref_continuous<S>;
+      auto shared = shared_of<S>(pars, n_groups);
+      std::vector<typename T::internal_state> internal(n_groups);
+      dust2::ode::control<double> ctl(max_steps, atol, rtol, step_size_min,
+                                      step_size_max, {}, false, false);
+      dust2::dust_continuous<T> sys(shared, internal, time_start, 0, ctl,
+                                    n_particles, seed, true, 1);
+      dust2::unfilter<dust2::dust_continuous<T>> obj(sys, time_start, tt,
+                                                     data_of(tag<S>{}));
+      finish(obj);
+      return 0;
+    }
+    bool ok = dispatch_discrete(name, [&](auto t, auto s) {
+      using T = typename decltype(t)::type;
+      using S = typename decltype(s)::type;
+      if constexpr (dust2gpu::has_compare_data<S>::value) {
+        auto shared = shared_of<S>(pars, n_groups);
+        std::vector<typename T::internal_state> internal(n_groups);
+        dust2::dust_discrete<T> sys(shared, internal, time_start, dt,
+                                    n_particles, seed, true, 1);
+        dust2::unfilter<dust2::dust_discrete<T>> obj(sys, time_start, tt,
+                                                     data_of(s));
+        finish(obj);
+      } else {
+        throw std::runtime_error("system has no compare_data");
+      }
+    });
+    if (!ok) {
       throw std::runtime_error("unknown system " + nm);
     }
     return 0;

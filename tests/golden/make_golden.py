@@ -9,6 +9,7 @@ numpy implementation in tests/xoshiro.py, so the fixtures do not depend
 on the engine under test.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(`--unfilter` writes only the deterministic-likelihood fixtures).
 """
 
 import sys
@@ -139,7 +140,36 @@ def main():
     r3, w3 = ref.scale_log_weights(np.array([-3.5]))
     save("filter_details", **cases, lw=lw, lw_ret=np.array([r1, r2, r3]),
          lw_w1=w1, lw_w2=w2, lw_w3=w3)
+    unfilters(ref)
+
+
+def unfilters(ref):
+    """8. Deterministic likelihoods (dust2::unfilter, test-unfilter.R):
+    a discrete SIR of 2 groups x 3 particles (dt = 0.25) and the sirode
+    ODE of 2 groups x 2 particles, data every 4 days with one missing
+    value, 2 runs each."""
+    times = np.arange(4, 41, 4, dtype=float)
+    rs = np.random.default_rng(8)
+    data = rs.poisson(8, 2 * times.size).astype(float)
+    data[5] = np.nan
+    pars = workload_data.sir_pars([
+        {"beta": 0.2, "gamma": 0.1, "N": 1000, "I0": 10},
+        {"beta": 0.3, "gamma": 0.15, "N": 2000, "I0": 5}])
+    ll, state = ref.unfilter_run("sir", pars, 2, 3, 0.0, times, data, 2, 5,
+                                 dt=0.25, n_runs=2)
+    save("unfilter_sir", pars=pars, times=times, data=data, ll=ll,
+         state=state)
+    pars = workload_data.pack("sirode", [
+        {"beta": 0.2, "gamma": 0.1, "N": 1000, "I0": 10},
+        {"beta": 0.3, "gamma": 0.15, "N": 2000, "I0": 5}])
+    ll, state = ref.unfilter_run("sirode", pars, 2, 2, 0.0, times, data, 2,
+                                 5, n_runs=2)
+    save("unfilter_sirode", pars=pars, times=times, data=data, ll=ll,
+         state=state)
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--unfilter"]:
+        unfilters(pyoracle.ref())
+    else:
+        main()

@@ -186,3 +186,14 @@ def test_port_errors_match_reference_engine(port, ref):
     assert str(e1.value) == str(e2.value)
     assert str(e1.value).startswith("10 particles reported errors.")
     assert "(and 6 more)" in str(e1.value)
+
+
+@pytest.mark.parametrize("name", ["sir", "sirode"])
+def test_port_unfilter_equals_reference_engine(port, name):
+    g = golden(f"unfilter_{name}")
+    n_particles = 3 if name == "sir" else 2
+    ll, state = port.unfilter_run(name, g["pars"], 2, n_particles, 0.0,
+                                  g["times"], g["data"], 2, 5, dt=0.25,
+                                  n_runs=2, n_threads=2)
+    np.testing.assert_array_equal(ll, g["ll"])
+    np.testing.assert_array_equal(state, g["state"])
