@@ -48,11 +48,13 @@ sys.path.insert(0, str(ROOT))
 # particle-step of the step+compare kernel, per workload, from the ncu SASS
 # counters of that kernel over a whole likelihood run (summaries under
 # profiles/).  A workload without an entry reports no achieved rate.
-FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 273.9, "ode_batched": 761.7}
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 273.9, "seir_batched": 4552.2,
+                              "ode_batched": 761.7}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
-FP64_PIPE_INST_PER_UNIT = {"sir_batched": 216.2, "ode_batched": 641.3}
+FP64_PIPE_INST_PER_UNIT = {"sir_batched": 216.2, "seir_batched": 3542.1,
+                           "ode_batched": 641.3}
 
 
 def pipe_roofline(workload, units_per_s, peak_tflops):
@@ -78,6 +80,9 @@ def parse_args():
                             "serve_seir", "ode_batched"])
     p.add_argument("--hbm-budget", type=float, default=16e9,
                    help="device memory budget of the likelihood server")
+    p.add_argument("--ode-instances", type=int, default=262144,
+                   help="instances of the dopri5 workload (smaller cases "
+                        "for profiling)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU sample")
@@ -580,6 +585,7 @@ def serve_arm(args, rank, world, local):
             "frac": None if achieved is None else achieved / peak,
             "traffic": None,
             "step_kernel_share": step_ms * 1e-3 / served_s,
+            "fp64_pipe": pipe_roofline("seir_batched", in_kernel_rate, peak),
             "flops_basis": "executed FP64 ops per particle-step of the "
                            "SEIR step kernel (ncu, seir_batched)"},
     }
@@ -643,7 +649,7 @@ def ode_arm(args, rank, world, local):
     from dust2_gb300 import _lib, workloads
 
     lib = _lib.lib()
-    w = workloads.sirode_batched()
+    w = workloads.sirode_batched(n_instances=args.ode_instances)
     G = w["n_groups"]
     times = _lib.as_f64(w["times"])
     h = ode_alloc(w)

@@ -718,6 +718,70 @@ int dust2_gb300_filter_set_rng_state(dust2_gb300_filter* filter,
   });
 }
 
+static std::vector<int> last_groups(dust2_gb300_filter* filter) {
+  std::vector<int> groups = filter->last_index_group;
+  if (groups.empty()) {
+    for (int g = 0; g < filter->impl->sys().n_groups(); ++g) {
+      groups.push_back(g);
+    }
+  }
+  return groups;
+}
+
+int dust2_gb300_filter_set_save_trajectories(dust2_gb300_filter* filter,
+                                             int32_t save,
+                                             const size_t* index_state,
+                                             size_t n_index_state) {
+  return guard([&] {
+    auto& f = filref(filter);
+    auto is = to_int_index(index_state, n_index_state, f.sys().n_state(),
+                           "index_state");
+    f.set_save_trajectories(save != 0, is.empty() ? nullptr : is.data(),
+                            static_cast<int>(is.size()));
+  });
+}
+
+int dust2_gb300_filter_trajectory_dim(dust2_gb300_filter* filter,
+                                      int32_t select_random_particle,
+                                      size_t* n_state, size_t* n_particles,
+                                      size_t* n_groups, size_t* n_time) {
+  return guard([&] {
+    auto& f = filref(filter);
+    need(f.trajectories_current(), "Trajectories are not current");
+    const auto groups = last_groups(filter);
+    *n_state = f.n_trajectory_state();
+    *n_particles = select_random_particle ? 1 :
+      f.sys().n_particles()[groups[0]];
+    *n_groups = groups.size();
+    *n_time = f.n_times();
+  });
+}
+
+int dust2_gb300_filter_last_trajectories(dust2_gb300_filter* filter,
+                                         int32_t select_random_particle,
+                                         double* out) {
+  return guard([&] {
+    auto& f = filref(filter);
+    need(f.trajectories_current(), "Trajectories are not current");
+    need(out != nullptr, "out is NULL");
+    const auto groups = last_groups(filter);
+    const auto& np = f.sys().n_particles();
+    for (int g : groups) {
+      need(np[g] == np[groups[0]],
+           "Trajectories need equal particle counts in every group");
+    }
+    std::vector<int> select;
+    if (select_random_particle) {
+      const auto pick = f.select_random_particle();
+      for (int g : groups) {
+        select.push_back(pick[g]);
+      }
+    }
+    f.last_trajectories(groups.data(), static_cast<int>(groups.size()),
+                        select.empty() ? nullptr : select.data(), out);
+  });
+}
+
 int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
                                   int32_t select_random_particle,
                                   double* out) {

@@ -140,6 +140,15 @@ public:
   virtual void set_timing(bool enable) = 0;
   virtual void kernel_times(double* step_ms, long* n_step_launches,
                             double* run_ms, long* n_runs) = 0;
+  // Save trajectories in the following runs (index_state: state entries,
+  // nullptr = all); export those of the last run for `groups`, all
+  // particles or select[i] of each, as [time][group][particle][state].
+  virtual void set_save_trajectories(bool save, const int* index_state,
+                                     int n_index_state) = 0;
+  virtual bool trajectories_current() const = 0;
+  virtual int n_trajectory_state() const = 0;
+  virtual void last_trajectories(const int* groups, int n_groups,
+                                 const int* select, double* out) = 0;
 };
 
 // The deterministic likelihood (dust2::unfilter, unfilter.hpp:10-73).

@@ -177,6 +177,17 @@ DUST2_PARTICLE_KERNEL(T) k_step_compare(system_view<T> v, filter_view f,
 __global__ void k_weights(filter_view f);
 __global__ void k_group(filter_view f, int n_groups);
 __global__ void k_resample(filter_view f);
+__global__ void k_save_history(const double* state, int stride,
+                               const int* index_state, int n_save,
+                               const tile* tiles, const int* active,
+                               const int* mode, const int* idx,
+                               double* hist_state, int* hist_order);
+__global__ void k_export_history(const double* hist_state,
+                                 const int* hist_order, int n_times,
+                                 int n_save, int stride,
+                                 const int* group_offset, const int* groups,
+                                 int n_groups_out, const int* select,
+                                 int n_particles_out, double* out);
 
 // Host-side description of the observation schedule.
 struct obs_step {
@@ -328,6 +339,90 @@ public:
     return static_cast<void*>(sys_->stream());
   }
 
+  // Trajectory saving (filter.hpp:89-100, trajectories.hpp): after each
+  // data time the post-reorder state (index_state entries, or all) and the
+  // resampling indices go to device history buffers.
+  void set_save_trajectories(bool save, const int* index_state,
+                             int n_index_state) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    std::vector<int> is;
+    if (save) {
+      const int n_state = sys_->n_state();
+      if (index_state == nullptr) {
+        for (int i = 0; i < n_state; ++i) {
+          is.push_back(i);
+        }
+      } else {
+        is.assign(index_state, index_state + n_index_state);
+      }
+    }
+    if (save != save_traj_ || is != traj_index_) {
+      save_traj_ = save;
+      traj_index_ = is;
+      graph_state_ptr_ = nullptr;  // force a re-capture
+      if (save) {
+        const std::size_t stride = sys_->layout().stride;
+        const std::size_t n_t = times_.size();
+        hist_state_.resize(n_t * is.size() * stride);
+        hist_order_.resize(n_t * stride);
+        traj_index_dev_.resize(is.size());
+        DUST2_CUDA(cudaMemcpy(traj_index_dev_.data(), is.data(),
+                              is.size() * sizeof(int),
+                              cudaMemcpyHostToDevice));
+      }
+    }
+  }
+
+  bool trajectories_current() const override {
+    return traj_current_;
+  }
+
+  int n_trajectory_state() const override {
+    return static_cast<int>(traj_index_.size());
+  }
+
+  // trajectories.hpp export_state with reorder = true: for each output
+  // particle (all, or select[i] of group groups[i]) walk its ancestry
+  // back from the last data time.  out: [time][group][particle][state].
+  void last_trajectories(const int* groups, int n_groups,
+                         const int* select, double* out) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    if (!traj_current_) {
+      throw std::runtime_error("Trajectories are not current");
+    }
+    const auto& L = sys_->layout();
+    const int n_particles = L.n_particles[groups[0]];
+    const int n_out = select != nullptr ? 1 : n_particles;
+    const int n_save = n_trajectory_state();
+    const int n_t = n_times();
+    const std::size_t len =
+      static_cast<std::size_t>(n_t) * n_groups * n_out * n_save;
+    device_array<double> buf(len);
+    device_array<int> g_dev(n_groups);
+    device_array<int> sel_dev(select != nullptr ? n_groups : 1);
+    auto s = sys_->stream();
+    DUST2_CUDA(cudaMemcpyAsync(g_dev.data(), groups, n_groups * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    if (select != nullptr) {
+      DUST2_CUDA(cudaMemcpyAsync(sel_dev.data(), select,
+                                 n_groups * sizeof(int),
+                                 cudaMemcpyHostToDevice, s));
+    }
+    const long n_threads = static_cast<long>(n_groups) * n_out;
+    k_export_history<<<n_blocks(n_threads, 128), 128, 0, s>>>(
+      hist_state_.data(), hist_order_.data(), n_t, n_save, L.stride,
+      offset_.data(), g_dev.data(), n_groups,
+      select != nullptr ? sel_dev.data() : nullptr, n_out, buf.data());
+    DUST2_CUDA(cudaGetLastError());
+    DUST2_CUDA(cudaMemcpyAsync(out, buf.data(), len * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    DUST2_CUDA(cudaStreamSynchronize(s));
+  }
+
   void set_timing(bool enable) override {
     if (enable != timing_) {
       if (pending_) {
@@ -366,6 +461,7 @@ public:
     if (pending_) {
       finish(nullptr);
     }
+    traj_current_ = false;
     active_host_.assign(G, index_group == nullptr ? 1 : 0);
     if (index_group != nullptr) {
       for (int i = 0; i < n_index_group; ++i) {
@@ -417,6 +513,7 @@ public:
     S.set_time(schedule_.empty() ? time_start_ : schedule_.back().t_compare);
     random_particle_.assign(G, -1);
     has_run_ = true;
+    traj_current_ = save_traj_;
   }
 
   void update_pars(const double* pars, const int* index_group,
@@ -564,6 +661,14 @@ private:
                                   L.tiles.empty() ? nullptr : S.tiles_dev(),
                                   offset_.data(), idx_.data(), mode_.data());
       std::swap(cur, other);
+      if (save_traj_) {
+        const std::size_t stride = L.stride;
+        k_save_history<<<NT, TS, 0, s>>>(
+          cur, L.stride, traj_index_dev_.data(), n_trajectory_state(),
+          S.tiles_dev(), active_.data(), mode_.data(), idx_.data(),
+          hist_state_.data() + i * traj_index_.size() * stride,
+          hist_order_.data() + i * stride);
+      }
     }
     if (cur != S.state_ptr()) {
       DUST2_CUDA(cudaMemcpyAsync(S.state_ptr(), cur,
@@ -653,6 +758,12 @@ private:
   bool pending_ = false;
   bool capturing_ = false;
   bool timing_ = false;
+  bool save_traj_ = false;
+  bool traj_current_ = false;
+  std::vector<int> traj_index_;
+  device_array<int> traj_index_dev_;
+  device_array<double> hist_state_;
+  device_array<int> hist_order_;
   long n_fallbacks_ = 0;
   std::vector<int> active_host_;
   int set_initial_host_ = 1;

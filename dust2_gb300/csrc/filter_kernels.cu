@@ -274,5 +274,54 @@ __global__ void k_fallback_count(filter_view f, int* count) {
   }
 }
 
+// After the reorder of a data time: the saved state entries of each
+// particle of the running groups, and where its state came from (the
+// group-local resampling index; itself when the group was not resampled).
+__global__ void k_save_history(const double* state, int stride,
+                               const int* index_state, int n_save,
+                               const tile* tiles, const int* active,
+                               const int* mode, const int* idx,
+                               double* hist_state, int* hist_order) {
+  const tile tl = tiles[blockIdx.x];
+  if (!active[tl.group] || static_cast<int>(threadIdx.x) >= tl.count) {
+    return;
+  }
+  const int k = tl.start + threadIdx.x;
+  for (int s = 0; s < n_save; ++s) {
+    hist_state[static_cast<long>(s) * stride + k] =
+      state[static_cast<long>(index_state[s]) * stride + k];
+  }
+  hist_order[k] = mode[tl.group] == MODE_KEEP ? tl.local + threadIdx.x :
+    idx[k];
+}
+
+// trajectories.hpp:135-190 (export_state with reorder): one thread per
+// output particle walks back through the saved indices from the last data
+// time.  out: [time][group][particle][state].
+__global__ void k_export_history(const double* hist_state,
+                                 const int* hist_order, int n_times,
+                                 int n_save, int stride,
+                                 const int* group_offset, const int* groups,
+                                 int n_groups_out, const int* select,
+                                 int n_particles_out, double* out) {
+  const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long>(n_groups_out) * n_particles_out) {
+    return;
+  }
+  const int go = static_cast<int>(t / n_particles_out);
+  const int jo = static_cast<int>(t % n_particles_out);
+  const int base = group_offset[groups[go]];
+  int j = select != nullptr ? select[go] : jo;
+  for (int i = n_times - 1; i >= 0; --i) {
+    const double* hs = hist_state + static_cast<long>(i) * n_save * stride;
+    double* dst = out + ((static_cast<long>(i) * n_groups_out + go) *
+                         n_particles_out + jo) * n_save;
+    for (int s = 0; s < n_save; ++s) {
+      dst[s] = hs[static_cast<long>(s) * stride + base + j];
+    }
+    j = hist_order[static_cast<long>(i) * stride + base + j];
+  }
+}
+
 }  // namespace engine
 }  // namespace dust2gpu

@@ -926,8 +926,9 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
                         index_state=None, index_group=None):
     """R/interface-likelihood.R:48-114, r/filter.hpp:112-143."""
     _check_lik(obj)
-    if save_trajectories:
-        raise DustError("save_trajectories is not supported by this engine")
+    if save_trajectories and isinstance(obj, DustUnfilter):
+        raise DustError("save_trajectories is not supported for unfilters "
+                        "by this engine")
     ig = _check_index(index_group, obj.n_groups, "index_group", unique=True)
     if pars is not None:
         pars = _check_pars(pars, obj.n_groups,
@@ -978,6 +979,12 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
         if obj.preserve_group_dimension:
             return ll[0, :]
         return float(ll[0, 0])
+    ist = None
+    if save_trajectories:
+        ist = _check_index(index_state, obj.n_state, "index_state")
+    check(_lib.lib().dust2_gb300_filter_set_save_trajectories(
+        obj.ptr, 1 if save_trajectories else 0, sptr(ist),
+        0 if ist is None else ist.size))
     ll = np.empty(n_out)
     check(_lib.lib().dust2_gb300_filter_run(
         obj.ptr, dptr(init), sptr(ig), 0 if ig is None else ig.size,
@@ -985,6 +992,31 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
     if not obj.preserve_group_dimension:
         return float(ll[0])
     return ll
+
+
+def dust_likelihood_last_trajectories(obj, select_random_particle=False):
+    """R/interface-likelihood.R dust_likelihood_last_trajectories,
+    r/filter.hpp:55-96: array (state, particle, group, time) with dust2's
+    dimension dropping."""
+    _check_lik(obj)
+    if obj.ptr is None or isinstance(obj, DustUnfilter):
+        raise DustError("Trajectories are not current")
+    dims = [ctypes.c_size_t() for _ in range(4)]
+    sel = 1 if select_random_particle else 0
+    check(_lib.lib().dust2_gb300_filter_trajectory_dim(
+        obj.ptr, sel, *[ctypes.byref(x) for x in dims]))
+    n_state, n_particles, n_groups, n_time = [x.value for x in dims]
+    out = np.empty(n_state * n_particles * n_groups * n_time)
+    check(_lib.lib().dust2_gb300_filter_last_trajectories(obj.ptr, sel,
+                                                          dptr(out)))
+    if select_random_particle:
+        shape = ((n_state, n_groups, n_time) if obj.preserve_group_dimension
+                 else (n_state, n_groups * n_time))
+    elif obj.preserve_group_dimension:
+        shape = (n_state, n_particles, n_groups, n_time)
+    else:
+        shape = (n_state, n_particles * n_groups, n_time)
+    return out.reshape(shape, order="F")
 
 
 def dust_likelihood_rng_state(obj):

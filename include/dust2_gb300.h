@@ -262,6 +262,34 @@ int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
                                   int32_t select_random_particle,
                                   double* out);
 
+/* Save trajectories in the following runs (filter.hpp:89-100, the
+ * save_trajectories / index_state arguments of dust2_filter_<sys>_run,
+ * r/filter.hpp:22-52): save = 1 or 0; index_state (NULL = all) selects
+ * the state entries kept. */
+int dust2_gb300_filter_set_save_trajectories(dust2_gb300_filter* filter,
+                                             int32_t save,
+                                             const size_t* index_state,
+                                             size_t n_index_state);
+
+/* Shape of dust2_gb300_filter_last_trajectories: saved state entries,
+ * particles per group (1 with select_random_particle), groups of the last
+ * run's index_group, data times. */
+int dust2_gb300_filter_trajectory_dim(dust2_gb300_filter* filter,
+                                      int32_t select_random_particle,
+                                      size_t* n_state, size_t* n_particles,
+                                      size_t* n_groups, size_t* n_time);
+
+/* dust2_filter_<sys>_last_trajectories (r/filter.hpp:55-96): the last
+ * run's trajectories with each particle's ancestry followed back through
+ * the resampling (trajectories.hpp:135-190), state fastest, then
+ * particle, group, time; with select_random_particle one particle per
+ * group (as dust2_gb300_filter_last_state).  Fails with "Trajectories are
+ * not current" unless the last run saved them.  Groups must have equal
+ * particle counts. */
+int dust2_gb300_filter_last_trajectories(dust2_gb300_filter* filter,
+                                         int32_t select_random_particle,
+                                         double* out);
+
 /* Groups whose resampling was recomputed serially so far (diagnostic of
  * the exact-resampling check). */
 int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,

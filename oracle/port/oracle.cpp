@@ -322,6 +322,12 @@ struct filter_port {
   int n_groups_data;
   std::vector<rng_t> frng;
   std::vector<double> ll;
+  // trajectories (filter.hpp:89-100): per data time the post-reorder
+  // state entries index_state of every particle, and the indices
+  bool save = false;
+  std::vector<int> index_state;
+  std::vector<std::vector<double>> hist_state;
+  std::vector<std::vector<size_t>> hist_order;
 
   static std::vector<uint64_t> system_words(const uint64_t* rng,
                                             const std::vector<int>& np) {
@@ -394,6 +400,40 @@ struct filter_port {
         }
       }
       sys.reorder(index, active);
+      if (save) {
+        std::vector<double> st;
+        for (size_t k = 0; k < sys.n_total; ++k) {
+          for (int j : index_state) {
+            st.push_back(sys.state[k * sys.n_state + j]);
+          }
+        }
+        hist_state.push_back(st);
+        hist_order.push_back(index);
+      }
+    }
+  }
+
+  // trajectories.hpp:135-190: each output particle of each group (all, or
+  // select[g]) followed back through the saved indices.
+  // out: [time][group][particle][state]
+  void export_trajectories(const int* select, double* out) const {
+    const size_t n_t = hist_state.size();
+    const size_t ns = index_state.size();
+    const size_t G = sys.n_particles.size();
+    size_t n_out = select != nullptr ? 1 : sys.n_particles[0];
+    for (size_t g = 0; g < G; ++g) {
+      for (size_t jo = 0; jo < n_out; ++jo) {
+        size_t j = select != nullptr ? select[g] : jo;
+        for (size_t irev = 0; irev < n_t; ++irev) {
+          const size_t i = n_t - 1 - irev;
+          const size_t k = sys.offset[g] + j;
+          double* dst = out + ((i * G + g) * n_out + jo) * ns;
+          for (size_t s2 = 0; s2 < ns; ++s2) {
+            dst[s2] = hist_state[i][k * ns + s2];
+          }
+          j = hist_order[i][k];
+        }
+      }
     }
   }
 };
@@ -996,6 +1036,51 @@ int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
     });
     if (!ok) {
       throw std::runtime_error("unknown system " + nm);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// One filter run saving trajectories of state entries index_state (all
+// when n_index_state is 0), then their export with reordering (select:
+// -1 for every particle, else the particle kept in each group).
+// out: [time][group][particle][state]
+int oracle_filter_trajectories(const char* name, const double* pars,
+                               int n_groups, int n_particles,
+                               double time_start, const double* times,
+                               int n_times, const double* data,
+                               int n_groups_data, double dt,
+                               const uint64_t* rng, const int* index_state,
+                               int n_index_state, const int* select,
+                               double* ll_out, double* out, int n_threads,
+                               char* err, int err_len) {
+  try {
+    bool ok = dispatch_discrete(name, [&](auto t) {
+      using S = typename decltype(t)::type;
+      if constexpr (dust2gpu::has_compare_data<S>::value) {
+        std::vector<int> np(n_groups, n_particles);
+        filter_port<S> f(shared_of<S>(pars, n_groups), np, time_start, times,
+                         n_times, data, n_groups_data, dt, rng, n_threads);
+        f.save = true;
+        if (n_index_state > 0) {
+          f.index_state.assign(index_state, index_state + n_index_state);
+        } else {
+          for (int j = 0; j < f.sys.n_state; ++j) {
+            f.index_state.push_back(j);
+          }
+        }
+        f.run(nullptr, std::vector<char>(n_groups, 1));
+        std::copy(f.ll.begin(), f.ll.end(), ll_out);
+        f.export_trajectories(select, out);
+      } else {
+        throw std::runtime_error("system has no compare_data");
+      }
+    });
+    if (!ok) {
+      throw std::runtime_error(std::string("unknown system ") + name);
     }
     return 0;
   } catch (const std::exception& e) {

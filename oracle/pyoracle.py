@@ -188,6 +188,49 @@ class Oracle:
         self._call(self._unf, *args)
         return ll.reshape(n_runs, n_groups, n_particles), state
 
+    def filter_trajectories(self, name, pars, n_groups, n_particles,
+                            time_start, times, data, n_groups_data, dt, rng,
+                            n_state_saved, index_state=None, select=None,
+                            select_random=False, n_threads=1):
+        """One filter run saving trajectories, exported with reordering:
+        (ll [group], trajectories [time][group][particle][state], select).
+        The port takes `select` (particle per group); the reference draws
+        it (select_random) and returns it."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        rng = np.ascontiguousarray(rng, dtype=np.uint64)
+        ist = (np.zeros(0, dtype=np.int32) if index_state is None else
+               np.ascontiguousarray(index_state, dtype=np.int32))
+        n_out = 1 if (select is not None or select_random) else n_particles
+        ll = np.empty(n_groups)
+        out = np.empty(times.size * n_groups * n_out * n_state_saved)
+        ip = ctypes.POINTER(ctypes.c_int)
+        if self.kind == "port":
+            sel = (None if select is None else
+                   np.ascontiguousarray(select, dtype=np.int32))
+            self._call(self.lib.oracle_filter_trajectories,
+                       _c(name.encode()), _dp(pars), _n(n_groups),
+                       _n(n_particles), ctypes.c_double(time_start),
+                       _dp(times), _n(times.size), _dp(data),
+                       _n(n_groups_data), ctypes.c_double(dt),
+                       rng.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                       ist.ctypes.data_as(ip), _n(ist.size),
+                       None if sel is None else sel.ctypes.data_as(ip),
+                       _dp(ll), _dp(out), _n(n_threads))
+            return ll, out, sel
+        sel = np.zeros(n_groups, dtype=np.int32)
+        self._call(self.lib.ref_filter_trajectories,
+                   _c(name.encode()), _dp(pars), _n(n_groups),
+                   _n(n_particles), ctypes.c_double(time_start), _dp(times),
+                   _n(times.size), _dp(data), _n(n_groups_data),
+                   ctypes.c_double(dt),
+                   rng.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                   ist.ctypes.data_as(ip), _n(ist.size),
+                   _n(1 if select_random else 0), _dp(ll), _dp(out),
+                   sel.ctypes.data_as(ip))
+        return ll, out, (sel if select_random else None)
+
     def scale_log_weights(self, w):
         w = np.array(w, dtype=np.float64)
         ret = self._slw(w.size, w.ctypes.data_as(_d))

@@ -418,6 +418,70 @@ int ref_ode_simulate(const char* name, const double* pars, int n_groups,
   }
 }
 
+// dust2::filter::run with save_trajectories (filter.hpp:42-104) and the
+// export of its trajectories with reordering (trajectories.hpp:135-190,
+// as r/filter.hpp:55-96 calls it); select_random draws one particle per
+// group from the filter's second streams (filter.hpp:130-138).
+// out: [time][group][particle][state]
+int ref_filter_trajectories(const char* name, const double* pars,
+                            int n_groups, int n_particles, double time_start,
+                            const double* times, int n_times,
+                            const double* data, int n_groups_data,
+                            double dt, const uint64_t* rng,
+                            const int* index_state, int n_index_state,
+                            int select_random, double* ll_out, double* out,
+                            int* select_out, char* err, int err_len) {
+  try {
+    bool ok = dispatch_discrete(name, [&](auto t, auto s) {
+      using T = typename decltype(t)::type;
+      using S = typename decltype(s)::type;
+      if constexpr (dust2gpu::has_compare_data<S>::value) {
+        auto shared = shared_of<S>(pars, n_groups);
+        std::vector<typename T::internal_state> internal(n_groups);
+        std::vector<uint64_t> seed_filter, seed_system;
+        for (int g = 0; g < n_groups; ++g) {
+          const uint64_t* it = rng + static_cast<size_t>(g) * 4 *
+            (n_particles + 2);
+          seed_filter.insert(seed_filter.end(), it, it + 8);
+          seed_system.insert(seed_system.end(), it + 8,
+                             it + 4 * (n_particles + 2));
+        }
+        dust2::dust_discrete<T> sys(shared, internal, time_start, dt,
+                                    n_particles, seed_system, false, 1);
+        std::vector<double> tt(times, times + n_times);
+        std::vector<typename S::data_type> d;
+        const int nd = sizeof(typename S::data_type) / sizeof(double);
+        for (int i = 0; i < n_times * n_groups_data; ++i) {
+          d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+        }
+        dust2::filter<dust2::dust_discrete<T>> obj(sys, time_start, tt, d,
+                                                   seed_filter);
+        std::vector<size_t> is(index_state, index_state + n_index_state);
+        obj.run(true, true, {}, is, obj.sys.all_groups());
+        const auto& ll = obj.last_log_likelihood();
+        std::copy(ll.begin(), ll.end(), ll_out);
+        std::vector<size_t> select;
+        if (select_random) {
+          select = obj.select_random_particle(obj.sys.all_groups());
+          for (int g = 0; g < n_groups; ++g) {
+            select_out[g] = static_cast<int>(select[g]);
+          }
+        }
+        obj.last_trajectories().export_state(out, true, select);
+      } else {
+        throw std::runtime_error("system has no compare_data");
+      }
+    });
+    if (!ok) {
+      throw std::runtime_error(std::string("unknown system ") + name);
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
 // dust2::unfilter (unfilter.hpp:42-73) on a deterministic system seeded
 // 42, as r/discrete/unfilter.hpp and r/continuous/unfilter.hpp build it;
 // n_runs runs at the same parameters.  ll_out: [n_runs][group][particle];

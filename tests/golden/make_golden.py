@@ -9,7 +9,7 @@ numpy implementation in tests/xoshiro.py, so the fixtures do not depend
 on the engine under test.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(`--unfilter` writes only the deterministic-likelihood fixtures).
+(`--unfilter` / `--trajectories` write only those fixtures).
 """
 
 import sys
@@ -141,6 +141,7 @@ def main():
     save("filter_details", **cases, lw=lw, lw_ret=np.array([r1, r2, r3]),
          lw_w1=w1, lw_w2=w2, lw_w3=w3)
     unfilters(ref)
+    trajectories(ref)
 
 
 def unfilters(ref):
@@ -168,8 +169,33 @@ def unfilters(ref):
          state=state)
 
 
+def trajectories(ref):
+    """9. Filter trajectories with reordering (test-filter.R "can save
+    trajectories from filter"): sir, 2 groups x 50 particles, all state,
+    state entries 2 and 4 (0-based 1 and 3), and one random particle per
+    group."""
+    pars = workload_data.sir_pars([
+        {"beta": 0.1, "gamma": 0.2, "N": 1000, "I0": 10, "exp_noise": 1e6},
+        {"beta": 0.2, "gamma": 0.2, "N": 1000, "I0": 10, "exp_noise": 1e6}])
+    n = 50
+    rng = xoshiro.streams(7, 2 * (n + 2))
+    times = np.array([4.0, 8, 12, 16, 20])
+    data = np.array([1.0, 2, 2, 3, 3, 4, 4, 5, 6, 6])
+    ll, full, _ = ref.filter_trajectories("sir", pars, 2, n, 0.0, times,
+                                          data, 2, 1.0, rng, 5)
+    _, sub, _ = ref.filter_trajectories("sir", pars, 2, n, 0.0, times, data,
+                                        2, 1.0, rng, 2, index_state=[1, 3])
+    _, one, sel = ref.filter_trajectories("sir", pars, 2, n, 0.0, times,
+                                          data, 2, 1.0, rng, 5,
+                                          select_random=True)
+    save("trajectories_sir", pars=pars, n_particles=n, rng=rng, times=times,
+         data=data, ll=ll, full=full, sub=sub, one=one, select=sel)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["--unfilter"]:
         unfilters(pyoracle.ref())
+    elif sys.argv[1:] == ["--trajectories"]:
+        trajectories(pyoracle.ref())
     else:
         main()

@@ -197,3 +197,16 @@ def test_port_unfilter_equals_reference_engine(port, name):
                                   n_runs=2, n_threads=2)
     np.testing.assert_array_equal(ll, g["ll"])
     np.testing.assert_array_equal(state, g["state"])
+
+
+def test_port_trajectories_equal_reference_engine(port):
+    g = golden("trajectories_sir")
+    args = ("sir", g["pars"], 2, int(g["n_particles"]), 0.0, g["times"],
+            g["data"], 2, 1.0, g["rng"])
+    ll, full, _ = port.filter_trajectories(*args, 5)
+    np.testing.assert_array_equal(ll, g["ll"])
+    np.testing.assert_array_equal(full, g["full"])
+    _, sub, _ = port.filter_trajectories(*args, 2, index_state=[1, 3])
+    np.testing.assert_array_equal(sub, g["sub"])
+    _, one, _ = port.filter_trajectories(*args, 5, select=g["select"])
+    np.testing.assert_array_equal(one, g["one"])
