@@ -7,7 +7,8 @@ from .interface import (
     DustLikelihood, DustServer, DustSystem, DustUnfilter, Generator,
     dust_filter_create,
     dust_filter_data, dust_likelihood_last_state, dust_likelihood_rng_state,
-    dust_likelihood_last_trajectories, dust_likelihood_run,
+    dust_likelihood_last_snapshots, dust_likelihood_last_trajectories,
+    dust_likelihood_run,
     dust_likelihood_serial_fallbacks, dust_likelihood_server, dust_likelihood_set_rng_state, dust_ode_control,
     dust_system_compare_data, dust_system_create, dust_system_internals,
     dust_system_reorder, dust_system_rng_state, dust_system_run_to_time,
@@ -22,7 +23,8 @@ __all__ = [
     "DustError", "DustLikelihood", "DustServer", "DustSystem",
     "DustUnfilter", "Generator",
     "device_count", "dust_filter_create", "dust_filter_data",
-    "dust_likelihood_last_state", "dust_likelihood_last_trajectories",
+    "dust_likelihood_last_snapshots", "dust_likelihood_last_state",
+    "dust_likelihood_last_trajectories",
     "dust_likelihood_rng_state",
     "dust_likelihood_run", "dust_likelihood_serial_fallbacks",
     "dust_likelihood_server", "dust_likelihood_set_rng_state",

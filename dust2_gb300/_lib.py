@@ -143,6 +143,13 @@ _SIGNATURES = {
         c_size_p]),
     "dust2_gb300_filter_last_trajectories": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32, c_double_p]),
+    "dust2_gb300_filter_set_save_snapshots": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, ctypes.c_size_t]),
+    "dust2_gb300_filter_snapshot_dim": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, c_size_p, c_size_p, c_size_p,
+        c_size_p]),
+    "dust2_gb300_filter_last_snapshots": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, c_double_p]),
     "dust2_gb300_unfilter_alloc": (ctypes.c_int, [
         ctypes.c_char_p, c_double_p, ctypes.c_size_t, ctypes.c_size_t,
         ctypes.c_double, c_double_p, ctypes.c_size_t, c_double_p,

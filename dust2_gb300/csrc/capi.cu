@@ -782,6 +782,60 @@ int dust2_gb300_filter_last_trajectories(dust2_gb300_filter* filter,
   });
 }
 
+int dust2_gb300_filter_set_save_snapshots(dust2_gb300_filter* filter,
+                                          const size_t* time_index,
+                                          size_t n) {
+  return guard([&] {
+    auto& f = filref(filter);
+    auto idx = to_int_index(time_index, n, f.n_times(), "save_snapshots");
+    for (std::size_t i = 1; i < idx.size(); ++i) {
+      need(idx[i] > idx[i - 1], "'save_snapshots' must be increasing");
+    }
+    f.set_save_snapshots(idx.data(), static_cast<int>(idx.size()));
+  });
+}
+
+int dust2_gb300_filter_snapshot_dim(dust2_gb300_filter* filter,
+                                    int32_t select_random_particle,
+                                    size_t* n_state, size_t* n_particles,
+                                    size_t* n_groups, size_t* n_snapshots) {
+  return guard([&] {
+    auto& f = filref(filter);
+    need(f.snapshots_current(), "Snapshots are not current");
+    const auto groups = last_groups(filter);
+    *n_state = f.sys().n_state();
+    *n_particles = select_random_particle ? 1 :
+      f.sys().n_particles()[groups[0]];
+    *n_groups = groups.size();
+    *n_snapshots = f.n_snapshots();
+  });
+}
+
+int dust2_gb300_filter_last_snapshots(dust2_gb300_filter* filter,
+                                      int32_t select_random_particle,
+                                      double* out) {
+  return guard([&] {
+    auto& f = filref(filter);
+    need(f.snapshots_current(), "Snapshots are not current");
+    need(out != nullptr, "out is NULL");
+    const auto groups = last_groups(filter);
+    const auto& np = f.sys().n_particles();
+    for (int g : groups) {
+      need(np[g] == np[groups[0]],
+           "Snapshots need equal particle counts in every group");
+    }
+    std::vector<int> select;
+    if (select_random_particle) {
+      const auto pick = f.select_random_particle();
+      for (int g : groups) {
+        select.push_back(pick[g]);
+      }
+    }
+    f.last_snapshots(groups.data(), static_cast<int>(groups.size()),
+                     select.empty() ? nullptr : select.data(), out);
+  });
+}
+
 int dust2_gb300_filter_last_state(dust2_gb300_filter* filter,
                                   int32_t select_random_particle,
                                   double* out) {

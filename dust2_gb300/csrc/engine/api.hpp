@@ -149,6 +149,12 @@ public:
   virtual int n_trajectory_state() const = 0;
   virtual void last_trajectories(const int* groups, int n_groups,
                                  const int* select, double* out) = 0;
+  // Snapshots of the full state at the data times with these indices.
+  virtual void set_save_snapshots(const int* obs, int n_obs) = 0;
+  virtual bool snapshots_current() const = 0;
+  virtual int n_snapshots() const = 0;
+  virtual void last_snapshots(const int* groups, int n_groups,
+                              const int* select, double* out) = 0;
 };
 
 // The deterministic likelihood (dust2::unfilter, unfilter.hpp:10-73).

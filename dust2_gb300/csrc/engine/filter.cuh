@@ -182,6 +182,13 @@ __global__ void k_save_history(const double* state, int stride,
                                const tile* tiles, const int* active,
                                const int* mode, const int* idx,
                                double* hist_state, int* hist_order);
+__global__ void k_export_snapshots(const double* snap_state,
+                                   const int* hist_order, int n_times,
+                                   const int* snap_obs, int n_snap,
+                                   int n_state, int stride,
+                                   const int* group_offset, const int* groups,
+                                   int n_groups_out, const int* select,
+                                   int n_particles_out, double* out);
 __global__ void k_export_history(const double* hist_state,
                                  const int* hist_order, int n_times,
                                  int n_save, int stride,
@@ -375,6 +382,89 @@ public:
     }
   }
 
+  // Snapshots (filter.hpp:89-100, trajectories.hpp:84-97): the full
+  // state after the reorder of the data times with these indices
+  // (increasing).
+  void set_save_snapshots(const int* obs, int n_obs) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    std::vector<int> v(obs, obs + n_obs);
+    if (v != snap_obs_) {
+      snap_obs_ = v;
+      graph_state_ptr_ = nullptr;  // force a re-capture
+      if (!v.empty()) {
+        const std::size_t stride = sys_->layout().stride;
+        const int n_state = sys_->n_state();
+        snap_state_.resize(v.size() * n_state * stride);
+        snap_obs_dev_.resize(v.size());
+        DUST2_CUDA(cudaMemcpy(snap_obs_dev_.data(), v.data(),
+                              v.size() * sizeof(int),
+                              cudaMemcpyHostToDevice));
+        std::vector<int> all(n_state);
+        for (int i = 0; i < n_state; ++i) {
+          all[i] = i;
+        }
+        all_state_dev_.resize(n_state);
+        DUST2_CUDA(cudaMemcpy(all_state_dev_.data(), all.data(),
+                              n_state * sizeof(int), cudaMemcpyHostToDevice));
+      }
+    }
+    if (!v.empty()) {
+      const std::size_t stride = sys_->layout().stride;
+      if (hist_order_.size() < times_.size() * stride) {
+        hist_order_.resize(times_.size() * stride);
+      }
+    }
+  }
+
+  bool snapshots_current() const override {
+    return snap_current_;
+  }
+
+  int n_snapshots() const override {
+    return static_cast<int>(snap_obs_.size());
+  }
+
+  // trajectories.hpp:199-268 (export_snapshots with reorder).
+  // out: [snapshot][group][particle][state]
+  void last_snapshots(const int* groups, int n_groups, const int* select,
+                      double* out) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    if (!snap_current_) {
+      throw std::runtime_error("Snapshots are not current");
+    }
+    const auto& L = sys_->layout();
+    const int n_particles = L.n_particles[groups[0]];
+    const int n_out = select != nullptr ? 1 : n_particles;
+    const int n_state = sys_->n_state();
+    const int n_snap = n_snapshots();
+    const std::size_t len =
+      static_cast<std::size_t>(n_snap) * n_groups * n_out * n_state;
+    device_array<double> buf(len);
+    device_array<int> g_dev(n_groups);
+    device_array<int> sel_dev(select != nullptr ? n_groups : 1);
+    auto s = sys_->stream();
+    DUST2_CUDA(cudaMemcpyAsync(g_dev.data(), groups, n_groups * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    if (select != nullptr) {
+      DUST2_CUDA(cudaMemcpyAsync(sel_dev.data(), select,
+                                 n_groups * sizeof(int),
+                                 cudaMemcpyHostToDevice, s));
+    }
+    const long n_threads = static_cast<long>(n_groups) * n_out;
+    k_export_snapshots<<<n_blocks(n_threads, 128), 128, 0, s>>>(
+      snap_state_.data(), hist_order_.data(), n_times(), snap_obs_dev_.data(),
+      n_snap, n_state, L.stride, offset_.data(), g_dev.data(), n_groups,
+      select != nullptr ? sel_dev.data() : nullptr, n_out, buf.data());
+    DUST2_CUDA(cudaGetLastError());
+    DUST2_CUDA(cudaMemcpyAsync(out, buf.data(), len * sizeof(double),
+                               cudaMemcpyDeviceToHost, s));
+    DUST2_CUDA(cudaStreamSynchronize(s));
+  }
+
   bool trajectories_current() const override {
     return traj_current_;
   }
@@ -462,6 +552,7 @@ public:
       finish(nullptr);
     }
     traj_current_ = false;
+    snap_current_ = false;
     active_host_.assign(G, index_group == nullptr ? 1 : 0);
     if (index_group != nullptr) {
       for (int i = 0; i < n_index_group; ++i) {
@@ -514,6 +605,7 @@ public:
     random_particle_.assign(G, -1);
     has_run_ = true;
     traj_current_ = save_traj_;
+    snap_current_ = !snap_obs_.empty();
   }
 
   void update_pars(const double* pars, const int* index_group,
@@ -661,13 +753,22 @@ private:
                                   L.tiles.empty() ? nullptr : S.tiles_dev(),
                                   offset_.data(), idx_.data(), mode_.data());
       std::swap(cur, other);
-      if (save_traj_) {
-        const std::size_t stride = L.stride;
+      const std::size_t stride = L.stride;
+      if (save_traj_ || !snap_obs_.empty()) {
         k_save_history<<<NT, TS, 0, s>>>(
-          cur, L.stride, traj_index_dev_.data(), n_trajectory_state(),
-          S.tiles_dev(), active_.data(), mode_.data(), idx_.data(),
-          hist_state_.data() + i * traj_index_.size() * stride,
-          hist_order_.data() + i * stride);
+          cur, L.stride, traj_index_dev_.data(),
+          save_traj_ ? n_trajectory_state() : 0, S.tiles_dev(),
+          active_.data(), mode_.data(), idx_.data(),
+          save_traj_ ? hist_state_.data() + i * traj_index_.size() * stride :
+          nullptr, hist_order_.data() + i * stride);
+      }
+      for (std::size_t sn = 0; sn < snap_obs_.size(); ++sn) {
+        if (snap_obs_[sn] == static_cast<int>(i)) {
+          k_save_history<<<NT, TS, 0, s>>>(
+            cur, L.stride, all_state_dev_.data(), S.n_state(),
+            S.tiles_dev(), active_.data(), mode_.data(), idx_.data(),
+            snap_state_.data() + sn * S.n_state() * stride, nullptr);
+        }
       }
     }
     if (cur != S.state_ptr()) {
@@ -764,6 +865,11 @@ private:
   device_array<int> traj_index_dev_;
   device_array<double> hist_state_;
   device_array<int> hist_order_;
+  std::vector<int> snap_obs_;
+  bool snap_current_ = false;
+  device_array<int> snap_obs_dev_;
+  device_array<int> all_state_dev_;
+  device_array<double> snap_state_;
   long n_fallbacks_ = 0;
   std::vector<int> active_host_;
   int set_initial_host_ = 1;

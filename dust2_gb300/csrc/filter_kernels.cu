@@ -291,8 +291,43 @@ __global__ void k_save_history(const double* state, int stride,
     hist_state[static_cast<long>(s) * stride + k] =
       state[static_cast<long>(index_state[s]) * stride + k];
   }
-  hist_order[k] = mode[tl.group] == MODE_KEEP ? tl.local + threadIdx.x :
-    idx[k];
+  if (hist_order != nullptr) {
+    hist_order[k] = mode[tl.group] == MODE_KEEP ? tl.local + threadIdx.x :
+      idx[k];
+  }
+}
+
+// trajectories.hpp:199-268 (export_snapshots with reorder): as
+// k_export_history, writing only at the snapshot data times.
+// out: [snapshot][group][particle][state]
+__global__ void k_export_snapshots(const double* snap_state,
+                                   const int* hist_order, int n_times,
+                                   const int* snap_obs, int n_snap,
+                                   int n_state, int stride,
+                                   const int* group_offset, const int* groups,
+                                   int n_groups_out, const int* select,
+                                   int n_particles_out, double* out) {
+  const long t = static_cast<long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long>(n_groups_out) * n_particles_out) {
+    return;
+  }
+  const int go = static_cast<int>(t / n_particles_out);
+  const int jo = static_cast<int>(t % n_particles_out);
+  const int base = group_offset[groups[go]];
+  int j = select != nullptr ? select[go] : jo;
+  int sn = n_snap - 1;
+  for (int i = n_times - 1; i >= 0 && sn >= 0; --i) {
+    if (snap_obs[sn] == i) {
+      const double* ss = snap_state + static_cast<long>(sn) * n_state * stride;
+      double* dst = out + ((static_cast<long>(sn) * n_groups_out + go) *
+                           n_particles_out + jo) * n_state;
+      for (int s = 0; s < n_state; ++s) {
+        dst[s] = ss[static_cast<long>(s) * stride + base + j];
+      }
+      --sn;
+    }
+    j = hist_order[static_cast<long>(i) * stride + base + j];
+  }
 }
 
 // trajectories.hpp:135-190 (export_state with reorder): one thread per

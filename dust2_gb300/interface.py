@@ -923,12 +923,27 @@ def _check_lik(obj):
 
 
 def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
-                        index_state=None, index_group=None):
+                        index_state=None, index_group=None,
+                        save_snapshots=None):
     """R/interface-likelihood.R:48-114, r/filter.hpp:112-143."""
     _check_lik(obj)
-    if save_trajectories and isinstance(obj, DustUnfilter):
+    if ((save_trajectories or save_snapshots is not None)
+            and isinstance(obj, DustUnfilter)):
         raise DustError("save_trajectories is not supported for unfilters "
                         "by this engine")
+    snap_index = None
+    if save_snapshots is not None:
+        # R/interface-likelihood.R:83-92
+        snaps = np.atleast_1d(np.asarray(save_snapshots, dtype=float))
+        if snaps.size > 1 and np.any(np.diff(snaps) <= 0):
+            raise DustError("'save_snapshots' must be increasing")
+        times = np.asarray(obj.data["time"], dtype=float)
+        ok = np.isin(snaps, times)
+        if not np.all(ok):
+            bad = ", ".join(f"{v:g}" for v in snaps[~ok])
+            raise DustError("All elements of 'save_snapshots' must be found "
+                            f"in 'time' (invalid: {bad})")
+        snap_index = as_size(np.searchsorted(times, snaps))
     ig = _check_index(index_group, obj.n_groups, "index_group", unique=True)
     if pars is not None:
         pars = _check_pars(pars, obj.n_groups,
@@ -985,6 +1000,9 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
     check(_lib.lib().dust2_gb300_filter_set_save_trajectories(
         obj.ptr, 1 if save_trajectories else 0, sptr(ist),
         0 if ist is None else ist.size))
+    check(_lib.lib().dust2_gb300_filter_set_save_snapshots(
+        obj.ptr, sptr(snap_index), 0 if snap_index is None else
+        snap_index.size))
     ll = np.empty(n_out)
     check(_lib.lib().dust2_gb300_filter_run(
         obj.ptr, dptr(init), sptr(ig), 0 if ig is None else ig.size,
@@ -992,6 +1010,30 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
     if not obj.preserve_group_dimension:
         return float(ll[0])
     return ll
+
+
+def dust_likelihood_last_snapshots(obj, select_random_particle=False):
+    """R/interface-likelihood.R:255-266, r/filter.hpp:98-137: array
+    (state, particle, group, snapshot) with dust2's dimension dropping."""
+    _check_lik(obj)
+    if obj.ptr is None or isinstance(obj, DustUnfilter):
+        raise DustError("Snapshots are not current")
+    dims = [ctypes.c_size_t() for _ in range(4)]
+    sel = 1 if select_random_particle else 0
+    check(_lib.lib().dust2_gb300_filter_snapshot_dim(
+        obj.ptr, sel, *[ctypes.byref(x) for x in dims]))
+    n_state, n_particles, n_groups, n_snap = [x.value for x in dims]
+    out = np.empty(n_state * n_particles * n_groups * n_snap)
+    check(_lib.lib().dust2_gb300_filter_last_snapshots(obj.ptr, sel,
+                                                       dptr(out)))
+    if select_random_particle:
+        shape = ((n_state, n_groups, n_snap) if obj.preserve_group_dimension
+                 else (n_state, n_groups * n_snap))
+    elif obj.preserve_group_dimension:
+        shape = (n_state, n_particles, n_groups, n_snap)
+    else:
+        shape = (n_state, n_particles * n_groups, n_snap)
+    return out.reshape(shape, order="F")
 
 
 def dust_likelihood_last_trajectories(obj, select_random_particle=False):

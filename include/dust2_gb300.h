@@ -290,6 +290,31 @@ int dust2_gb300_filter_last_trajectories(dust2_gb300_filter* filter,
                                          int32_t select_random_particle,
                                          double* out);
 
+/* Save snapshots of the full state in the following runs
+ * (save_snapshots of dust2_filter_<sys>_run; trajectories.hpp:84-97) at
+ * the data times with these 0-based indices (increasing; n = 0 stops
+ * saving).  The R layer maps snapshot times to indices and rejects times
+ * not in the data (R/interface-likelihood.R:83-92). */
+int dust2_gb300_filter_set_save_snapshots(dust2_gb300_filter* filter,
+                                          const size_t* time_index,
+                                          size_t n);
+
+/* Shape of dust2_gb300_filter_last_snapshots: state entries, particles
+ * per group (1 with select_random_particle), groups, snapshots. */
+int dust2_gb300_filter_snapshot_dim(dust2_gb300_filter* filter,
+                                    int32_t select_random_particle,
+                                    size_t* n_state, size_t* n_particles,
+                                    size_t* n_groups, size_t* n_snapshots);
+
+/* dust2_filter_<sys>_last_snapshots (r/filter.hpp:98-137): the saved
+ * states with ancestry followed back through the resampling
+ * (trajectories.hpp:199-268); layout and random particle as
+ * dust2_gb300_filter_last_trajectories.  Fails with "Snapshots are not
+ * current" unless the last run saved them. */
+int dust2_gb300_filter_last_snapshots(dust2_gb300_filter* filter,
+                                      int32_t select_random_particle,
+                                      double* out);
+
 /* Groups whose resampling was recomputed serially so far (diagnostic of
  * the exact-resampling check). */
 int dust2_gb300_filter_serial_fallbacks(dust2_gb300_filter* filter,

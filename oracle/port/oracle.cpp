@@ -328,6 +328,8 @@ struct filter_port {
   std::vector<int> index_state;
   std::vector<std::vector<double>> hist_state;
   std::vector<std::vector<size_t>> hist_order;
+  std::vector<int> snap_obs;  // data time indices of snapshots
+  std::vector<std::vector<double>> snaps;
 
   static std::vector<uint64_t> system_words(const uint64_t* rng,
                                             const std::vector<int>& np) {
@@ -409,6 +411,37 @@ struct filter_port {
         }
         hist_state.push_back(st);
         hist_order.push_back(index);
+      }
+      if (std::find(snap_obs.begin(), snap_obs.end(),
+                    static_cast<int>(it)) != snap_obs.end()) {
+        snaps.push_back(sys.state);
+      }
+    }
+  }
+
+  // trajectories.hpp:199-268 with reorder: out [snapshot][group]
+  // [particle][state]
+  void export_snapshots(const int* select, double* out) const {
+    const size_t n_t = hist_order.size();
+    const size_t ns = sys.n_state;
+    const size_t G = sys.n_particles.size();
+    size_t n_out = select != nullptr ? 1 : sys.n_particles[0];
+    for (size_t g = 0; g < G; ++g) {
+      for (size_t jo = 0; jo < n_out; ++jo) {
+        size_t j = select != nullptr ? select[g] : jo;
+        long sn = static_cast<long>(snap_obs.size()) - 1;
+        for (size_t irev = 0; irev < n_t && sn >= 0; ++irev) {
+          const size_t i = n_t - 1 - irev;
+          const size_t k = sys.offset[g] + j;
+          if (snap_obs[sn] == static_cast<int>(i)) {
+            double* dst = out + ((sn * G + g) * n_out + jo) * ns;
+            for (size_t s2 = 0; s2 < ns; ++s2) {
+              dst[s2] = snaps[sn][k * ns + s2];
+            }
+            --sn;
+          }
+          j = hist_order[i][k];
+        }
       }
     }
   }
@@ -1054,9 +1087,10 @@ int oracle_filter_trajectories(const char* name, const double* pars,
                                int n_times, const double* data,
                                int n_groups_data, double dt,
                                const uint64_t* rng, const int* index_state,
-                               int n_index_state, const int* select,
-                               double* ll_out, double* out, int n_threads,
-                               char* err, int err_len) {
+                               int n_index_state, const int* snap_obs,
+                               int n_snap, const int* select,
+                               double* ll_out, double* out, double* snap_out,
+                               int n_threads, char* err, int err_len) {
   try {
     bool ok = dispatch_discrete(name, [&](auto t) {
       using S = typename decltype(t)::type;
@@ -1072,9 +1106,13 @@ int oracle_filter_trajectories(const char* name, const double* pars,
             f.index_state.push_back(j);
           }
         }
+        f.snap_obs.assign(snap_obs, snap_obs + n_snap);
         f.run(nullptr, std::vector<char>(n_groups, 1));
         std::copy(f.ll.begin(), f.ll.end(), ll_out);
         f.export_trajectories(select, out);
+        if (n_snap > 0) {
+          f.export_snapshots(select, snap_out);
+        }
       } else {
         throw std::runtime_error("system has no compare_data");
       }

@@ -191,11 +191,14 @@ class Oracle:
     def filter_trajectories(self, name, pars, n_groups, n_particles,
                             time_start, times, data, n_groups_data, dt, rng,
                             n_state_saved, index_state=None, select=None,
-                            select_random=False, n_threads=1):
-        """One filter run saving trajectories, exported with reordering:
-        (ll [group], trajectories [time][group][particle][state], select).
-        The port takes `select` (particle per group); the reference draws
-        it (select_random) and returns it."""
+                            select_random=False, snapshots=None, n_state=5,
+                            n_threads=1):
+        """One filter run saving trajectories (and snapshots at the data
+        times `snapshots`), exported with reordering: (ll [group],
+        trajectories [time][group][particle][state], select, snapshots
+        [snapshot][group][particle][state]).  The port takes `select`
+        (particle per group); the reference draws it (select_random) and
+        returns it."""
         pars = np.ascontiguousarray(pars, dtype=np.float64)
         times = np.ascontiguousarray(times, dtype=np.float64)
         data = np.ascontiguousarray(data, dtype=np.float64)
@@ -206,6 +209,11 @@ class Oracle:
         ll = np.empty(n_groups)
         out = np.empty(times.size * n_groups * n_out * n_state_saved)
         ip = ctypes.POINTER(ctypes.c_int)
+        snaps = (np.zeros(0) if snapshots is None else
+                 np.ascontiguousarray(snapshots, dtype=np.float64))
+        snap_obs = np.ascontiguousarray(np.searchsorted(times, snaps),
+                                        dtype=np.int32)
+        snap_out = np.empty(max(1, snaps.size * n_groups * n_out * n_state))
         if self.kind == "port":
             sel = (None if select is None else
                    np.ascontiguousarray(select, dtype=np.int32))
@@ -216,9 +224,11 @@ class Oracle:
                        _n(n_groups_data), ctypes.c_double(dt),
                        rng.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
                        ist.ctypes.data_as(ip), _n(ist.size),
+                       snap_obs.ctypes.data_as(ip), _n(snap_obs.size),
                        None if sel is None else sel.ctypes.data_as(ip),
-                       _dp(ll), _dp(out), _n(n_threads))
-            return ll, out, sel
+                       _dp(ll), _dp(out), _dp(snap_out), _n(n_threads))
+            return ll, out, sel, snap_out[:snaps.size * n_groups * n_out *
+                                          n_state]
         sel = np.zeros(n_groups, dtype=np.int32)
         self._call(self.lib.ref_filter_trajectories,
                    _c(name.encode()), _dp(pars), _n(n_groups),
@@ -226,10 +236,11 @@ class Oracle:
                    _n(times.size), _dp(data), _n(n_groups_data),
                    ctypes.c_double(dt),
                    rng.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
-                   ist.ctypes.data_as(ip), _n(ist.size),
-                   _n(1 if select_random else 0), _dp(ll), _dp(out),
-                   sel.ctypes.data_as(ip))
-        return ll, out, (sel if select_random else None)
+                   ist.ctypes.data_as(ip), _n(ist.size), _dp(snaps),
+                   _n(snaps.size), _n(1 if select_random else 0), _dp(ll),
+                   _dp(out), _dp(snap_out), sel.ctypes.data_as(ip))
+        return (ll, out, (sel if select_random else None),
+                snap_out[:snaps.size * n_groups * n_out * n_state])
 
     def scale_log_weights(self, w):
         w = np.array(w, dtype=np.float64)

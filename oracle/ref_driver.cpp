@@ -418,19 +418,22 @@ int ref_ode_simulate(const char* name, const double* pars, int n_groups,
   }
 }
 
-// dust2::filter::run with save_trajectories (filter.hpp:42-104) and the
-// export of its trajectories with reordering (trajectories.hpp:135-190,
-// as r/filter.hpp:55-96 calls it); select_random draws one particle per
-// group from the filter's second streams (filter.hpp:130-138).
-// out: [time][group][particle][state]
+// dust2::filter::run with save_trajectories and snapshots
+// (filter.hpp:42-104) and the export of both with reordering
+// (trajectories.hpp:135-268, as r/filter.hpp:55-137 calls it);
+// select_random draws one particle per group from the filter's second
+// streams (filter.hpp:130-138).  out: [time][group][particle][state];
+// snap_out: [snapshot][group][particle][state]
 int ref_filter_trajectories(const char* name, const double* pars,
                             int n_groups, int n_particles, double time_start,
                             const double* times, int n_times,
                             const double* data, int n_groups_data,
                             double dt, const uint64_t* rng,
                             const int* index_state, int n_index_state,
+                            const double* snapshots, int n_snapshots,
                             int select_random, double* ll_out, double* out,
-                            int* select_out, char* err, int err_len) {
+                            double* snap_out, int* select_out, char* err,
+                            int err_len) {
   try {
     bool ok = dispatch_discrete(name, [&](auto t, auto s) {
       using T = typename decltype(t)::type;
@@ -457,7 +460,8 @@ int ref_filter_trajectories(const char* name, const double* pars,
         dust2::filter<dust2::dust_discrete<T>> obj(sys, time_start, tt, d,
                                                    seed_filter);
         std::vector<size_t> is(index_state, index_state + n_index_state);
-        obj.run(true, true, {}, is, obj.sys.all_groups());
+        std::vector<double> snaps(snapshots, snapshots + n_snapshots);
+        obj.run(true, true, snaps, is, obj.sys.all_groups());
         const auto& ll = obj.last_log_likelihood();
         std::copy(ll.begin(), ll.end(), ll_out);
         std::vector<size_t> select;
@@ -468,6 +472,9 @@ int ref_filter_trajectories(const char* name, const double* pars,
           }
         }
         obj.last_trajectories().export_state(out, true, select);
+        if (n_snapshots > 0) {
+          obj.last_trajectories().export_snapshots(snap_out, true, select);
+        }
       } else {
         throw std::runtime_error("system has no compare_data");
       }

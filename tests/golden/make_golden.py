@@ -170,10 +170,10 @@ def unfilters(ref):
 
 
 def trajectories(ref):
-    """9. Filter trajectories with reordering (test-filter.R "can save
-    trajectories from filter"): sir, 2 groups x 50 particles, all state,
-    state entries 2 and 4 (0-based 1 and 3), and one random particle per
-    group."""
+    """9. Filter trajectories and snapshots with reordering (test-filter.R
+    "can save trajectories from filter", "can save snapshots"): sir, 2
+    groups x 50 particles, all state, state entries 2 and 4 (0-based 1 and
+    3), one random particle per group, snapshots at times 8 and 16."""
     pars = workload_data.sir_pars([
         {"beta": 0.1, "gamma": 0.2, "N": 1000, "I0": 10, "exp_noise": 1e6},
         {"beta": 0.2, "gamma": 0.2, "N": 1000, "I0": 10, "exp_noise": 1e6}])
@@ -181,15 +181,19 @@ def trajectories(ref):
     rng = xoshiro.streams(7, 2 * (n + 2))
     times = np.array([4.0, 8, 12, 16, 20])
     data = np.array([1.0, 2, 2, 3, 3, 4, 4, 5, 6, 6])
-    ll, full, _ = ref.filter_trajectories("sir", pars, 2, n, 0.0, times,
-                                          data, 2, 1.0, rng, 5)
-    _, sub, _ = ref.filter_trajectories("sir", pars, 2, n, 0.0, times, data,
-                                        2, 1.0, rng, 2, index_state=[1, 3])
-    _, one, sel = ref.filter_trajectories("sir", pars, 2, n, 0.0, times,
-                                          data, 2, 1.0, rng, 5,
-                                          select_random=True)
+    snapshots = np.array([8.0, 16.0])
+    ll, full, _, snap = ref.filter_trajectories(
+        "sir", pars, 2, n, 0.0, times, data, 2, 1.0, rng, 5,
+        snapshots=snapshots)
+    _, sub, _, _ = ref.filter_trajectories(
+        "sir", pars, 2, n, 0.0, times, data, 2, 1.0, rng, 2,
+        index_state=[1, 3])
+    _, one, sel, snap_one = ref.filter_trajectories(
+        "sir", pars, 2, n, 0.0, times, data, 2, 1.0, rng, 5,
+        select_random=True, snapshots=snapshots)
     save("trajectories_sir", pars=pars, n_particles=n, rng=rng, times=times,
-         data=data, ll=ll, full=full, sub=sub, one=one, select=sel)
+         data=data, ll=ll, full=full, sub=sub, one=one, select=sel,
+         snapshots=snapshots, snap=snap, snap_one=snap_one)
 
 
 if __name__ == "__main__":

@@ -89,3 +89,33 @@ def test_trajectories_end_at_last_state(built):
     traj = d.dust_likelihood_last_trajectories(obj)
     last = d.dust_likelihood_last_state(obj)
     np.testing.assert_array_equal(traj[..., -1], last)
+
+
+def test_snapshots_match_reference(built):
+    g = golden("trajectories_sir")
+    obj = make(g)
+    d.dust_likelihood_run(obj, plist(g), save_snapshots=g["snapshots"])
+    with pytest.raises(d.DustError, match="Trajectories are not current"):
+        d.dust_likelihood_last_trajectories(obj)
+    snap = d.dust_likelihood_last_snapshots(obj)
+    assert snap.shape == (5, int(g["n_particles"]), 2, 2)
+    np.testing.assert_array_equal(as_fixture(snap), g["snap"])
+    one = d.dust_likelihood_last_snapshots(obj, select_random_particle=True)
+    want = g["snap_one"].reshape(2, 2, 5)
+    np.testing.assert_array_equal(np.transpose(one, (2, 1, 0)), want)
+
+
+def test_snapshots_with_trajectories_and_validation(built):
+    g = golden("trajectories_sir")
+    obj = make(g)
+    d.dust_likelihood_run(obj, plist(g), save_trajectories=True,
+                          save_snapshots=g["snapshots"])
+    np.testing.assert_array_equal(
+        as_fixture(d.dust_likelihood_last_trajectories(obj)), g["full"])
+    np.testing.assert_array_equal(
+        as_fixture(d.dust_likelihood_last_snapshots(obj)), g["snap"])
+    with pytest.raises(d.DustError, match="must be found in 'time'"):
+        d.dust_likelihood_run(obj, None, save_snapshots=[5.0])
+    d.dust_likelihood_run(obj, None)
+    with pytest.raises(d.DustError, match="Snapshots are not current"):
+        d.dust_likelihood_last_snapshots(obj)

@@ -203,10 +203,14 @@ def test_port_trajectories_equal_reference_engine(port):
     g = golden("trajectories_sir")
     args = ("sir", g["pars"], 2, int(g["n_particles"]), 0.0, g["times"],
             g["data"], 2, 1.0, g["rng"])
-    ll, full, _ = port.filter_trajectories(*args, 5)
+    ll, full, _, snap = port.filter_trajectories(
+        *args, 5, snapshots=g["snapshots"])
     np.testing.assert_array_equal(ll, g["ll"])
     np.testing.assert_array_equal(full, g["full"])
-    _, sub, _ = port.filter_trajectories(*args, 2, index_state=[1, 3])
+    np.testing.assert_array_equal(snap, g["snap"])
+    _, sub, _, _ = port.filter_trajectories(*args, 2, index_state=[1, 3])
     np.testing.assert_array_equal(sub, g["sub"])
-    _, one, _ = port.filter_trajectories(*args, 5, select=g["select"])
+    _, one, _, snap_one = port.filter_trajectories(
+        *args, 5, select=g["select"], snapshots=g["snapshots"])
     np.testing.assert_array_equal(one, g["one"])
+    np.testing.assert_array_equal(snap_one, g["snap_one"])
