@@ -180,6 +180,30 @@ constexpr int default_tile_size() {
   return T::n_state_max > 32 ? 128 : 256;
 }
 
+// The tile size for a set of groups: the system's block size, halved
+// (down to one warp) while that leaves fewer than two tiles per SM, so
+// that small problems spread over more of the GPU.  Results do not depend
+// on it: per-group sums use a fixed chunk structure (filter.cuh).
+template <typename T>
+int choose_tile_size(const std::vector<int>& n_particles) {
+  int dev = 0, sms = 0;
+  DUST2_CUDA(cudaGetDevice(&dev));
+  DUST2_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount,
+                                    dev));
+  auto n_tiles = [&](int ts) {
+    long n = 0;
+    for (int np : n_particles) {
+      n += (np + ts - 1) / ts;
+    }
+    return n;
+  };
+  int t = default_tile_size<T>();
+  while (t > 32 && n_tiles(t) < 2L * sms) {
+    t /= 2;
+  }
+  return t;
+}
+
 // Blocks per SM the per-particle kernels of a system must fit, which caps
 // registers per thread at 65536 / (tile size * blocks): a system may
 // declare `static constexpr int min_blocks_per_sm`; the default, 2, allows
@@ -306,7 +330,8 @@ public:
                   const std::vector<std::uint64_t>& rng_words,
                   bool deterministic, int tile_size = 0) :
     shared_(std::move(shared)),
-    layout_(n_particles, tile_size > 0 ? tile_size : default_tile_size<T>()),
+    layout_(n_particles,
+            tile_size > 0 ? tile_size : choose_tile_size<T>(n_particles)),
     n_state_(T::n_state(shared_[0])),
     time_(time), dt_(dt), deterministic_(deterministic) {
     if (static_cast<int>(shared_.size()) != layout_.n_groups) {

@@ -9,32 +9,35 @@
 //                      "any weight non-zero" flag (:71-72) and the maximum
 //                      log weight (filter_details.hpp:19-25; NaN counts as
 //                      -Inf).
-//   2. k_weights       one block per tile: w = exp(logw - max) and the
-//                      tile's inclusive prefix sums (FP64).
-//   3. k_group         one warp per group: scan of tile totals, the
+//   2. k_weights       w = exp(logw - max); one warp per 32-particle
+//                      chunk of a group: inclusive prefix sums and the
+//                      chunk total (FP64).
+//   3. k_group         one warp per group: scan of the chunk totals, the
 //                      log-likelihood increment log(sum/n) + max (:32-38),
 //                      and the uniform u from the group's filter stream 2g
 //                      (filter.hpp:75).
 //   4. k_resample      one thread per particle: systematic resampling
 //                      target uu_i = sum*u/n + i*sum/n and a search of the
 //                      prefix sums (filter_details.hpp:45-74).
-//   5. k_fallback      one warp per flagged group: the serial algorithm.
+//   5. k_fallback      one block per flagged group: the serial algorithm.
 //   6. k_reorder       gather of the resampled state (discrete/system.hpp
 //                      :170-181).
+//
+// The sums of steps 2-3 have a fixed structure (chunks of 32 particles,
+// then windows of 32 chunks with a carry) that does not depend on the
+// tile size, so neither the log-likelihood nor the indices do.
 //
 // Exactness of the resampling indices.  dust2 accumulates the weights
 // serially; a parallel scan rounds differently, so a search target that
 // falls within a few ulps of a cumulative boundary could pick a
 // neighbouring particle.  Step 4 therefore checks every decision against
-// a rigorous error bound: the serial and parallel prefix sums of n
-// non-negative weights (each within 2 ulp of the other side's exp) differ
-// by at most (n + log2 n + 6) u sum (u = 2^-53), and the targets, computed
-// from either total, by at most that plus 8 u sum.  A decision is accepted
-// only when both neighbouring prefix sums are farther than
-// (4n + 128) u sum from the target; otherwise the whole group is recomputed
-// serially (step 5), which is the reference algorithm verbatim.  The
+// a rigorous, position-dependent bound on the difference between the
+// serial and the parallel prefix sums (see k_resample); a decision is
+// accepted only when both neighbouring prefix sums are farther than that
+// from the target, otherwise the whole group is recomputed serially
+// (step 5), which is the reference algorithm verbatim.  The
 // log-likelihood uses the parallel total; it matches the serial one to
-// better than n u relative.
+// better than n u relative (u = 2^-53).
 //
 // The whole sequence for all data times is captured once into a CUDA
 // graph and replayed on every run.
@@ -69,13 +72,13 @@ struct filter_view {
   const int* active;          // [n_groups] 1 = run this group
   const int* n_particles;     // [n_groups]
   const int* offset;          // [n_groups]
-  const int* tile_first;      // [n_groups]
-  const int* tile_count;      // [n_groups]
+  const int* chunk_first;     // [n_groups] first 32-particle chunk
+  const int* chunk_count;     // [n_groups]
   double* w;                  // [n_total] raw log weights
   double* ew;                 // [n_total] exp(w - max)
   double* pre;                // [n_total] tile-local inclusive prefix
-  double* tile_sum;           // [n_tiles]
-  double* tile_off;           // [n_tiles] exclusive offsets within group
+  double* chunk_sum;          // [n_chunks] chunk totals of ew
+  double* chunk_off;          // [n_chunks] exclusive offsets within group
   unsigned long long* gkey;   // [n_groups] ordered key of max log weight
   int* gnz;                   // [n_groups] any weight != 0
   int* gflag;                 // [n_groups] ambiguous decision seen
@@ -174,6 +177,30 @@ DUST2_PARTICLE_KERNEL(T) k_step_compare(system_view<T> v, filter_view f,
                        data + (n_groups_data == 1 ? 0 : tl.group));
 }
 
+// Exclusive offsets of a group's chunks (warp scans of 32 chunk totals
+// and a running carry; the exclusive value comes from the neighbour
+// lane, so every offset is a plain sum); returns the group total.
+__device__ __forceinline__ double group_chunk_offsets(const filter_view& f,
+                                                      int g, int lane) {
+  const int c0 = f.chunk_first[g];
+  const int nc = f.chunk_count[g];
+  double carry = 0;
+  for (int base = 0; base < nc; base += 32) {
+    const int c = base + lane;
+    const double v = c < nc ? f.chunk_sum[c0 + c] : 0.0;
+    const double incl = warp_inclusive_scan(v);
+    double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+    if (lane == 0) {
+      excl = 0;
+    }
+    if (c < nc) {
+      f.chunk_off[c0 + c] = carry + excl;
+    }
+    carry = carry + __shfl_sync(0xffffffffu, incl, 31);
+  }
+  return carry;
+}
+
 __global__ void k_weights(filter_view f);
 __global__ void k_group(filter_view f, int n_groups);
 __global__ void k_resample(filter_view f);
@@ -230,13 +257,13 @@ public:
     active_.resize(G);
     n_part_.resize(G);
     offset_.resize(G);
-    tile_first_.resize(G);
-    tile_count_.resize(G);
+    chunk_first_.resize(G);
+    chunk_count_.resize(G);
     w_.resize(N);
     ew_.resize(N);
     pre_.resize(N);
-    tile_sum_.resize(NT);
-    tile_off_.resize(NT);
+    chunk_sum_.resize(L.n_chunks);
+    chunk_off_.resize(L.n_chunks);
     gkey_.resize(G);
     gnz_.resize(G);
     gflag_.resize(G);
@@ -259,9 +286,9 @@ public:
                                G * sizeof(int), cudaMemcpyHostToDevice, s));
     DUST2_CUDA(cudaMemcpyAsync(offset_.data(), L.offset.data(),
                                G * sizeof(int), cudaMemcpyHostToDevice, s));
-    DUST2_CUDA(cudaMemcpyAsync(tile_first_.data(), L.tile_first.data(),
+    DUST2_CUDA(cudaMemcpyAsync(chunk_first_.data(), L.chunk_first.data(),
                                G * sizeof(int), cudaMemcpyHostToDevice, s));
-    DUST2_CUDA(cudaMemcpyAsync(tile_count_.data(), L.tile_count.data(),
+    DUST2_CUDA(cudaMemcpyAsync(chunk_count_.data(), L.chunk_count.data(),
                                G * sizeof(int), cudaMemcpyHostToDevice, s));
     DUST2_CUDA(cudaMemcpyAsync(data_.data(), data.data(),
                                data.size() * sizeof(data_type),
@@ -302,9 +329,9 @@ public:
     const auto& L = sys_->layout();
     (void)L;
     return filter_view{sys_->tiles_dev(), active_.data(), n_part_.data(),
-                       offset_.data(), tile_first_.data(),
-                       tile_count_.data(), w_.data(), ew_.data(), pre_.data(),
-                       tile_sum_.data(), tile_off_.data(), gkey_.data(),
+                       offset_.data(), chunk_first_.data(),
+                       chunk_count_.data(), w_.data(), ew_.data(), pre_.data(),
+                       chunk_sum_.data(), chunk_off_.data(), gkey_.data(),
                        gnz_.data(), gflag_.data(), mode_.data(), ll_.data(),
                        gu_.data(), guu0_.data(), gdu_.data(), gtot_.data(),
                        idx_.data(), frng_.data(), set_initial_.data(),
@@ -881,8 +908,8 @@ private:
   long n_step_launches_ = 0;
   long n_timed_runs_ = 0;
 
-  device_array<int> active_, n_part_, offset_, tile_first_, tile_count_;
-  device_array<double> w_, ew_, pre_, tile_sum_, tile_off_;
+  device_array<int> active_, n_part_, offset_, chunk_first_, chunk_count_;
+  device_array<double> w_, ew_, pre_, chunk_sum_, chunk_off_;
   device_array<unsigned long long> gkey_;
   device_array<int> gnz_, gflag_, mode_;
   device_array<double> ll_, gu_, guu0_, gdu_, gtot_;

@@ -32,6 +32,11 @@ struct group_layout {
   std::vector<int> offset;       // global index of a group's first particle
   std::vector<int> tile_first;   // first tile of each group
   std::vector<int> tile_count;   // tiles in each group
+  // Chunks: runs of 32 particles of one group (warp-sized, group-local
+  // indices 32c .. 32c+31), the units of the filter's weight sums.
+  std::vector<int> chunk_first;  // first chunk of each group
+  std::vector<int> chunk_count;  // chunks in each group
+  int n_chunks = 0;
   std::vector<tile> tiles;
   // Packed tiles: consecutive runs of tile_size particles whatever their
   // group, used by the per-particle kernels that need no reduction over a
@@ -70,6 +75,9 @@ struct group_layout {
       tile_first.push_back(static_cast<int>(tiles.size()));
       const int nt = (n[g] + tile_size - 1) / tile_size;
       tile_count.push_back(nt);
+      chunk_first.push_back(n_chunks);
+      chunk_count.push_back((n[g] + 31) / 32);
+      n_chunks += (n[g] + 31) / 32;
       for (int t = 0; t < nt; ++t) {
         const int local = t * tile_size;
         const int count = std::min(tile_size, n[g] - local);

@@ -330,8 +330,10 @@ public:
     idx_.resize(P);
     errors_.resize(P);
     tiles_.resize(max_tiles_);
-    tile_sum_.resize(max_tiles_);
-    tile_off_.resize(max_tiles_);
+    // chunks of 32 particles: the pool's 32-aligned ranges hold at most
+    // capacity / 32 of them
+    chunk_sum_.resize(cap_particles_ / ALIGN + n_slots_);
+    chunk_off_.resize(cap_particles_ / ALIGN + n_slots_);
     shared_dev_.resize(S);
     zero_dev_.resize(S);
     slots_dev_.resize(S);
@@ -341,8 +343,8 @@ public:
     active_.resize(S);
     n_part_.resize(S);
     offset_.resize(S);
-    tile_first_.resize(S);
-    tile_count_.resize(S);
+    chunk_first_.resize(S);
+    chunk_count_.resize(S);
     gkey_.resize(S);
     gnz_.resize(S);
     gflag_.resize(S);
@@ -364,7 +366,7 @@ public:
     DUST2_CUDA(cudaMemsetAsync(errors_.data(), 0,
                                errors_.size() * sizeof(particle_error), s));
     for (auto* p : {&starting_, &slot_error_, &active_, &n_part_, &offset_,
-                    &tile_first_, &tile_count_, &gnz_, &gflag_, &mode_,
+                    &chunk_first_, &chunk_count_, &gnz_, &gflag_, &mode_,
                     &obs_dev_, &fallback_count_, &scalars_}) {
       DUST2_CUDA(cudaMemsetAsync(p->data(), 0, p->size() * sizeof(int), s));
     }
@@ -664,9 +666,10 @@ private:
 
   filter_view fview() {
     return filter_view{tiles_.data(), active_.data(), n_part_.data(),
-                       offset_.data(), tile_first_.data(), tile_count_.data(),
-                       w_.data(), ew_.data(), pre_.data(), tile_sum_.data(),
-                       tile_off_.data(), gkey_.data(), gnz_.data(),
+                       offset_.data(), chunk_first_.data(),
+                       chunk_count_.data(), w_.data(), ew_.data(), pre_.data(),
+                       chunk_sum_.data(), chunk_off_.data(), gkey_.data(),
+                       gnz_.data(),
                        gflag_.data(), mode_.data(), ll_.data(), gu_.data(),
                        guu0_.data(), gdu_.data(), gtot_.data(), idx_.data(),
                        frng_.data(), scalars_.data(), scalars_.data() + 1};
@@ -883,8 +886,9 @@ private:
   // Tiles over every resident session, grouped by slot.
   void rebuild_tiles() {
     std::vector<tile> tiles;
-    std::vector<int> np(n_slots_, 0), off(n_slots_, 0), tf(n_slots_, 0),
-      tc(n_slots_, 0);
+    std::vector<int> np(n_slots_, 0), off(n_slots_, 0), cf(n_slots_, 0),
+      cc(n_slots_, 0);
+    int n_chunks = 0;
     {
       std::lock_guard<std::mutex> lock(mu_);
       for (int s = 0; s < n_slots_; ++s) {
@@ -895,9 +899,10 @@ private:
         const session& ss = *sessions_.at(id);
         np[s] = ss.n;
         off[s] = static_cast<int>(ss.offset);
-        tf[s] = static_cast<int>(tiles.size());
+        cf[s] = n_chunks;
+        cc[s] = (ss.n + 31) / 32;
+        n_chunks += cc[s];
         const int nt = (ss.n + tile_size_ - 1) / tile_size_;
-        tc[s] = nt;
         for (int t = 0; t < nt; ++t) {
           const int local = t * tile_size_;
           tiles.push_back(tile{s, static_cast<int>(ss.offset) + local,
@@ -913,8 +918,8 @@ private:
     ring_.upload(tiles_.data(), tiles.data(), tiles.size() * sizeof(tile), s);
     ring_.upload(n_part_.data(), np.data(), np.size() * sizeof(int), s);
     ring_.upload(offset_.data(), off.data(), off.size() * sizeof(int), s);
-    ring_.upload(tile_first_.data(), tf.data(), tf.size() * sizeof(int), s);
-    ring_.upload(tile_count_.data(), tc.data(), tc.size() * sizeof(int), s);
+    ring_.upload(chunk_first_.data(), cf.data(), cf.size() * sizeof(int), s);
+    ring_.upload(chunk_count_.data(), cc.data(), cc.size() * sizeof(int), s);
   }
 
   // Start requests: parameters, then reset of the slot's filter state
@@ -1123,12 +1128,12 @@ private:
   device_array<int> idx_;
   device_array<particle_error> errors_;
   device_array<tile> tiles_;
-  device_array<double> tile_sum_, tile_off_;
+  device_array<double> chunk_sum_, chunk_off_;
   device_array<shared_state> shared_dev_;
   device_array<zero_every_spec> zero_dev_;
   device_array<served_slot> slots_dev_;
   device_array<int> obs_dev_, starting_, slot_error_;
-  device_array<int> active_, n_part_, offset_, tile_first_, tile_count_;
+  device_array<int> active_, n_part_, offset_, chunk_first_, chunk_count_;
   device_array<unsigned long long> gkey_;
   device_array<int> gnz_, gflag_, mode_;
   device_array<double> ll_, gu_, guu0_, gdu_, gtot_;

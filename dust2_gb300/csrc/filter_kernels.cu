@@ -24,9 +24,14 @@ __global__ void k_filter_reset(filter_view f, int n_groups) {
   f.mode[g] = MODE_KEEP;
 }
 
-// exp(w - max) and tile-local inclusive prefix sums.
+// Weight sums are built in a fixed structure that does not depend on how
+// particles are cut into tiles: each 32-particle chunk of a group (one
+// warp) is scanned by a warp scan, and each group's chunk totals by warp
+// scans of 32 chunks with a running carry.  The log-likelihood and the
+// resampling indices are therefore the same for any tile size.
+
+// exp(w - max), the chunk-local inclusive prefix sums and chunk totals.
 __global__ void k_weights(filter_view f) {
-  __shared__ double smem[33];
   const tile tl = f.tiles[blockIdx.x];
   const int g = tl.group;
   if (!f.active[g] || !f.gnz[g] || f.n_particles[g] == 1) {
@@ -36,6 +41,10 @@ __global__ void k_weights(filter_view f) {
   if (mx == -INFINITY) {
     return;
   }
+  const int warp = threadIdx.x >> 5;
+  if (32 * warp >= tl.count) {
+    return;  // the whole warp is past the tile's particles
+  }
   const bool valid = static_cast<int>(threadIdx.x) < tl.count;
   const int k = tl.start + threadIdx.x;
   double e = 0;
@@ -43,18 +52,17 @@ __global__ void k_weights(filter_view f) {
     const double w = f.w[k];
     e = (w != w) ? 0.0 : math::exp(w - mx);
   }
-  double total;
-  const double incl = block_inclusive_scan(e, smem, &total);
+  const double incl = warp_inclusive_scan(e);
   if (valid) {
     f.ew[k] = e;
     f.pre[k] = incl;
   }
-  if (threadIdx.x == 0) {
-    f.tile_sum[blockIdx.x] = total;
+  if ((threadIdx.x & 31) == 31) {
+    f.chunk_sum[f.chunk_first[g] + tl.local / 32 + warp] = incl;
   }
 }
 
-// One warp per group: tile offsets, log-likelihood increment and the
+// One warp per group: chunk offsets, log-likelihood increment and the
 // resampling uniform; then clear the per-observation reductions.
 __global__ void k_group(filter_view f, int n_groups) {
   const int g = blockIdx.x;
@@ -68,19 +76,7 @@ __global__ void k_group(filter_view f, int n_groups) {
   int mode = MODE_KEEP;
   double tot = 0;
   if (nz && n > 1 && mx != -INFINITY) {
-    const int t0 = f.tile_first[g];
-    const int nt = f.tile_count[g];
-    double carry = 0;
-    for (int base = 0; base < nt; base += 32) {
-      const int t = base + lane;
-      const double v = t < nt ? f.tile_sum[t0 + t] : 0.0;
-      const double incl = warp_inclusive_scan(v);
-      if (t < nt) {
-        f.tile_off[t0 + t] = carry + (incl - v);
-      }
-      carry = carry + __shfl_sync(0xffffffffu, incl, 31);
-    }
-    tot = carry;
+    tot = group_chunk_offsets(f, g, lane);
   }
   if (lane == 0) {
     if (nz) {
@@ -119,9 +115,8 @@ __global__ void k_group(filter_view f, int n_groups) {
 
 // Prefix sum Q_m (weights 0..m of the group) for group-local index m.
 __device__ __forceinline__ double prefix_at(const filter_view& f, int g,
-                                            int m, int tile_size) {
-  const int t = f.tile_first[g] + m / tile_size;
-  return f.tile_off[t] + f.pre[f.offset[g] + m];
+                                            int m) {
+  return f.chunk_off[f.chunk_first[g] + (m >> 5)] + f.pre[f.offset[g] + m];
 }
 
 __global__ void k_resample(filter_view f) {
@@ -140,29 +135,28 @@ __global__ void k_resample(filter_view f) {
     return;
   }
   const int n = f.n_particles[g];
-  const int ts = blockDim.x;
   const int i = tl.local + threadIdx.x;
-  const double tot = f.gtot[g];
   const double uu = f.guu0[g] + static_cast<double>(i) * f.gdu[g];
-  // first tile whose last prefix reaches uu
-  const int t0 = f.tile_first[g];
-  int lo = 0, hi = f.tile_count[g];
+  // first chunk whose last prefix reaches uu
+  const int c0 = f.chunk_first[g];
+  const int nc = f.chunk_count[g];
+  int lo = 0, hi = nc;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
-    if (f.tile_off[t0 + mid] + f.tile_sum[t0 + mid] >= uu) {
+    if (f.chunk_off[c0 + mid] + f.chunk_sum[c0 + mid] >= uu) {
       hi = mid;
     } else {
       lo = mid + 1;
     }
   }
   int m;
-  if (lo == f.tile_count[g]) {
+  if (lo == nc) {
     m = n - 1;  // past the end: the serial loop stops at j == n
   } else {
-    const int first = lo * ts;
-    const int last = min(n, first + ts) - 1;
+    const int first = lo * 32;
+    const int last = min(n, first + 32) - 1;
     int a = first, b = last;
-    const double off = f.tile_off[t0 + lo];
+    const double off = f.chunk_off[c0 + lo];
     const double* pre = f.pre + f.offset[g];
     while (a < b) {
       const int mid = (a + b) >> 1;
@@ -181,24 +175,26 @@ __global__ void k_resample(filter_view f) {
   // reaches it (needed only for m < n - 1: the loop stops at the last
   // particle anyway).
   //
-  // Bound, with u = 2^-53 and L = log2(n) + 2: a serial prefix of k
-  // weights differs from the exact sum S_k by at most (k - 1) u S_k; the
-  // block scan here by at most L u S_k; each weight may differ from the
-  // other side's exp by 2 ulp (4 u S_k); the target computed from either
-  // total differs by at most (n + L + 10) u uu.  So a decision is safe
-  // when the prefix is farther than (k + n + 2L + 16) u max(S_k, uu)
-  // from the target (5% slack on top).
-  // ceil(log2 n) on the integer pipe
-  const double L = 2.0 + (n > 1 ? 32 - __clz(n - 1) : 0);
+  // Bound, with u = 2^-53: a serial prefix of k weights differs from the
+  // exact sum S_k by at most (k - 1) u S_k.  A prefix here is a sum of
+  // non-negative terms by a tree of depth at most L = 18 + ceil(nc / 32)
+  // (5 levels within a chunk, 5 for the chunk total, 5 across a window
+  // of 32 chunks, one per earlier window, and the joins), so within
+  // L u S_k; each weight may differ from the other side's exp by 2 ulp
+  // (4 u S_k); the target computed from either total differs by at most
+  // (n + L + 10) u uu.  So a decision is safe when the prefix is farther
+  // than (k + n + 2L + 16) u max(S_k, uu) from the target (5% slack on
+  // top).
+  const double L = 18.0 + static_cast<double>((nc + 31) >> 5);
   const double eps = 0x1.0p-53 * 1.05;
   bool ok = true;
   if (m > 0) {
-    const double p = prefix_at(f, g, m - 1, ts);
+    const double p = prefix_at(f, g, m - 1);
     const double margin = eps * (m + n + 2 * L + 16) * fmax(p, uu);
     ok = ok && p < uu - margin;
   }
   if (m < n - 1) {
-    const double q = prefix_at(f, g, m, ts);
+    const double q = prefix_at(f, g, m);
     const double margin = eps * (m + 1 + n + 2 * L + 16) * fmax(q, uu);
     ok = ok && q >= uu + margin;
   }

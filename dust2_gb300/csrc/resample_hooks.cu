@@ -22,21 +22,23 @@
 namespace dust2gpu {
 namespace engine {
 
-// Tile scans of raw (already exponentiated) weights: ew = w.
+// Chunk scans of raw (already exponentiated) weights: ew = w.
 __global__ void k_weights_raw(filter_view f) {
-  __shared__ double smem[33];
   const tile tl = f.tiles[blockIdx.x];
+  const int warp = threadIdx.x >> 5;
+  if (32 * warp >= tl.count) {
+    return;
+  }
   const bool valid = static_cast<int>(threadIdx.x) < tl.count;
   const int k = tl.start + threadIdx.x;
   const double e = valid ? f.w[k] : 0.0;
-  double total;
-  const double incl = block_inclusive_scan(e, smem, &total);
+  const double incl = warp_inclusive_scan(e);
   if (valid) {
     f.ew[k] = e;
     f.pre[k] = incl;
   }
-  if (threadIdx.x == 0) {
-    f.tile_sum[blockIdx.x] = total;
+  if ((threadIdx.x & 31) == 31) {
+    f.chunk_sum[f.chunk_first[tl.group] + tl.local / 32 + warp] = incl;
   }
 }
 
@@ -64,19 +66,8 @@ __global__ void k_group_given_u(filter_view f, double u, int lse,
   const int g = 0;
   const int lane = threadIdx.x;
   const int n = f.n_particles[g];
-  const int nt = f.tile_count[g];
-  double carry = 0;
-  for (int base = 0; base < nt; base += 32) {
-    const int t = base + lane;
-    const double v = t < nt ? f.tile_sum[t] : 0.0;
-    const double incl = warp_inclusive_scan(v);
-    if (t < nt) {
-      f.tile_off[t] = carry + (incl - v);
-    }
-    carry = carry + __shfl_sync(0xffffffffu, incl, 31);
-  }
+  const double tot = group_chunk_offsets(f, g, lane);
   if (lane == 0) {
-    const double tot = carry;
     if (lse) {
       f.ll[g] = math::log(tot / n) + ordered_value(f.gkey[g]);
     }
@@ -91,9 +82,10 @@ __global__ void k_group_given_u(filter_view f, double u, int lse,
 
 std::size_t hook_scratch_bytes(std::size_t n, int tile_size) {
   const std::size_t nt = (n + tile_size - 1) / tile_size;
-  // w, ew, pre (n doubles each), tile_sum, tile_off (nt doubles each),
+  const std::size_t nc = (n + 31) / 32;
+  // w, ew, pre (n doubles each), chunk_sum, chunk_off (nc doubles each),
   // idx (n ints), tiles (nt), 7 doubles + 1 key + 8 ints of group data
-  return 256 * 16 + 3 * n * 8 + 2 * nt * 8 + n * 4 + nt * sizeof(tile) +
+  return 256 * 16 + 3 * n * 8 + 2 * nc * 8 + n * 4 + nt * sizeof(tile) +
     7 * 8 + 8 + 8 * 4;
 }
 
@@ -114,8 +106,9 @@ void hook_layout(char* base, std::size_t n, int tile_size,
   f.w = reinterpret_cast<double*>(take(n * 8));
   f.ew = reinterpret_cast<double*>(take(n * 8));
   f.pre = reinterpret_cast<double*>(take(n * 8));
-  f.tile_sum = reinterpret_cast<double*>(take(nt * 8));
-  f.tile_off = reinterpret_cast<double*>(take(nt * 8));
+  const std::size_t nc = (n + 31) / 32;
+  f.chunk_sum = reinterpret_cast<double*>(take(nc * 8));
+  f.chunk_off = reinterpret_cast<double*>(take(nc * 8));
   f.idx = reinterpret_cast<int*>(take(n * 4));
   tile* t_dev = reinterpret_cast<tile*>(take(nt * sizeof(tile)));
   double* dbl = reinterpret_cast<double*>(take(7 * 8));
@@ -129,8 +122,8 @@ void hook_layout(char* base, std::size_t n, int tile_size,
   f.active = ints;
   f.n_particles = ints + 1;
   f.offset = ints + 2;
-  f.tile_first = ints + 3;
-  f.tile_count = ints + 4;
+  f.chunk_first = ints + 3;
+  f.chunk_count = ints + 4;
   f.gnz = ints + 5;
   f.gflag = ints + 6;
   f.mode = ints + 7;
@@ -139,7 +132,7 @@ void hook_layout(char* base, std::size_t n, int tile_size,
   f.set_initial = nullptr;
   f.force_serial = nullptr;
   const int h_ints[8] = {1, static_cast<int>(n), 0, 0,
-                         static_cast<int>(nt), 0, 0, MODE_RESAMPLE};
+                         static_cast<int>(nc), 0, 0, MODE_RESAMPLE};
   DUST2_CUDA(cudaMemcpyAsync(ints, h_ints, sizeof(h_ints),
                              cudaMemcpyHostToDevice, s));
   const unsigned long long key0 = 0;  // below every ordered key

@@ -24,8 +24,9 @@ void hook_layout_fixed(char* base, std::size_t n, int tile_size,
   f.w = reinterpret_cast<double*>(take(n * 8));
   f.ew = reinterpret_cast<double*>(take(n * 8));
   f.pre = reinterpret_cast<double*>(take(n * 8));
-  f.tile_sum = reinterpret_cast<double*>(take(nt * 8));
-  f.tile_off = reinterpret_cast<double*>(take(nt * 8));
+  const std::size_t nc = (n + 31) / 32;
+  f.chunk_sum = reinterpret_cast<double*>(take(nc * 8));
+  f.chunk_off = reinterpret_cast<double*>(take(nc * 8));
   f.idx = reinterpret_cast<int*>(take(n * 4));
   tile* t_dev = reinterpret_cast<tile*>(take(nt * sizeof(tile)));
   double* dbl = reinterpret_cast<double*>(take(7 * 8));
@@ -39,8 +40,8 @@ void hook_layout_fixed(char* base, std::size_t n, int tile_size,
   f.active = ints;
   f.n_particles = ints + 1;
   f.offset = ints + 2;
-  f.tile_first = ints + 3;
-  f.tile_count = ints + 4;
+  f.chunk_first = ints + 3;
+  f.chunk_count = ints + 4;
   f.gnz = ints + 5;
   f.gflag = ints + 6;
   f.mode = ints + 7;
@@ -50,8 +51,8 @@ void hook_layout_fixed(char* base, std::size_t n, int tile_size,
   f.force_serial = nullptr;
   // every per-group scalar is rewritten here, so nothing left from an
   // earlier call in the same memory is read
-  const int h_ints[8] = {1, static_cast<int>(n), 0, 0, n_tiles, 0, 0,
-                         MODE_RESAMPLE};
+  const int h_ints[8] = {1, static_cast<int>(n), 0, 0,
+                         static_cast<int>(nc), 0, 0, MODE_RESAMPLE};
   DUST2_CUDA(cudaMemcpyAsync(ints, h_ints, sizeof(h_ints),
                              cudaMemcpyHostToDevice, s));
   const unsigned long long key0 = 0;
