@@ -6,7 +6,8 @@ from ._lib import DustError, device_count
 from .interface import (
     DustLikelihood, DustServer, DustSystem, DustUnfilter, Generator,
     dust_filter_create,
-    dust_filter_data, dust_likelihood_last_state, dust_likelihood_rng_state,
+    dust_filter_data, dust_likelihood_last_gradient,
+    dust_likelihood_last_state, dust_likelihood_rng_state,
     dust_likelihood_last_snapshots, dust_likelihood_last_trajectories,
     dust_likelihood_run,
     dust_likelihood_serial_fallbacks, dust_likelihood_server, dust_likelihood_set_rng_state, dust_ode_control,
@@ -23,6 +24,7 @@ __all__ = [
     "DustError", "DustLikelihood", "DustServer", "DustSystem",
     "DustUnfilter", "Generator",
     "device_count", "dust_filter_create", "dust_filter_data",
+    "dust_likelihood_last_gradient",
     "dust_likelihood_last_snapshots", "dust_likelihood_last_state",
     "dust_likelihood_last_trajectories",
     "dust_likelihood_rng_state",

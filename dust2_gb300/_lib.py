@@ -158,6 +158,24 @@ _SIGNATURES = {
     "dust2_gb300_unfilter_free": (ctypes.c_int, [ctypes.c_void_p]),
     "dust2_gb300_unfilter_run": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p, c_size_p, ctypes.c_size_t, c_double_p]),
+    "dust2_gb300_unfilter_run_adjoint": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p, c_size_p, ctypes.c_size_t, c_double_p]),
+    "dust2_gb300_unfilter_gradient_dim": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, c_size_p]),
+    "dust2_gb300_unfilter_last_gradient": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p]),
+    "dust2_gb300_unfilter_set_save_trajectories": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, c_size_p, ctypes.c_size_t]),
+    "dust2_gb300_unfilter_set_save_snapshots": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, ctypes.c_size_t]),
+    "dust2_gb300_unfilter_trajectory_dim": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, c_size_p, c_size_p, c_size_p]),
+    "dust2_gb300_unfilter_last_trajectories": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p]),
+    "dust2_gb300_unfilter_snapshot_dim": (ctypes.c_int, [
+        ctypes.c_void_p, c_size_p, c_size_p, c_size_p, c_size_p]),
+    "dust2_gb300_unfilter_last_snapshots": (ctypes.c_int, [
+        ctypes.c_void_p, c_double_p]),
     "dust2_gb300_unfilter_update_pars": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p, c_size_p, ctypes.c_size_t]),
     "dust2_gb300_unfilter_state": (ctypes.c_int, [ctypes.c_void_p,

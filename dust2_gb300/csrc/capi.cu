@@ -970,6 +970,116 @@ int dust2_gb300_unfilter_run(dust2_gb300_unfilter* unfilter,
   });
 }
 
+int dust2_gb300_unfilter_run_adjoint(dust2_gb300_unfilter* unfilter,
+                                     const double* initial,
+                                     const size_t* index_group,
+                                     size_t n_index_group, double* ll) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(ll != nullptr, "ll is NULL");
+    auto ig = to_int_index(index_group, n_index_group, u.sys().n_groups(),
+                           "index_group");
+    u.run_adjoint(initial, ig.empty() ? nullptr : ig.data(),
+                  static_cast<int>(ig.size()), ll);
+  });
+}
+
+int dust2_gb300_unfilter_gradient_dim(const dust2_gb300_unfilter* unfilter,
+                                      size_t* n_gradient,
+                                      size_t* n_groups_last) {
+  return guard([&] {
+    need(unfilter != nullptr && unfilter->impl != nullptr,
+         "Invalid unfilter handle");
+    need(n_gradient != nullptr && n_groups_last != nullptr,
+         "output is NULL");
+    *n_gradient = unfilter->impl->n_gradient();
+    *n_groups_last = unfilter->impl->n_last_gradient_groups();
+  });
+}
+
+int dust2_gb300_unfilter_last_gradient(dust2_gb300_unfilter* unfilter,
+                                       double* out) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(out != nullptr, "out is NULL");
+    need(u.n_gradient() > 0, "This system does not support adjoint methods");
+    u.last_gradient(out);
+  });
+}
+
+int dust2_gb300_unfilter_set_save_trajectories(dust2_gb300_unfilter* unfilter,
+                                               int32_t save,
+                                               const size_t* index_state,
+                                               size_t n_index_state) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    auto is = to_int_index(index_state, n_index_state, u.sys().n_state(),
+                           "index_state");
+    u.set_save_trajectories(save != 0, is.empty() ? nullptr : is.data(),
+                            static_cast<int>(is.size()));
+  });
+}
+
+int dust2_gb300_unfilter_set_save_snapshots(dust2_gb300_unfilter* unfilter,
+                                            const size_t* time_index,
+                                            size_t n) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    auto idx = to_int_index(time_index, n, u.n_times(), "save_snapshots");
+    for (std::size_t i = 1; i < idx.size(); ++i) {
+      need(idx[i] > idx[i - 1], "'save_snapshots' must be increasing");
+    }
+    u.set_save_snapshots(idx.data(), static_cast<int>(idx.size()));
+  });
+}
+
+int dust2_gb300_unfilter_trajectory_dim(dust2_gb300_unfilter* unfilter,
+                                        size_t* n_state, size_t* n_particles,
+                                        size_t* n_groups, size_t* n_time) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(u.trajectories_current(), "Trajectories are not current");
+    const auto& groups = u.saved_groups();
+    *n_state = u.n_trajectory_state();
+    *n_particles = u.sys().n_particles()[groups[0]];
+    *n_groups = groups.size();
+    *n_time = u.n_times();
+  });
+}
+
+int dust2_gb300_unfilter_last_trajectories(dust2_gb300_unfilter* unfilter,
+                                           double* out) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(out != nullptr, "out is NULL");
+    u.last_trajectories(out);
+  });
+}
+
+int dust2_gb300_unfilter_snapshot_dim(dust2_gb300_unfilter* unfilter,
+                                      size_t* n_state, size_t* n_particles,
+                                      size_t* n_groups,
+                                      size_t* n_snapshots) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(u.snapshots_current(), "Snapshots are not current");
+    const auto& groups = u.saved_groups();
+    *n_state = u.sys().n_state();
+    *n_particles = u.sys().n_particles()[groups[0]];
+    *n_groups = groups.size();
+    *n_snapshots = u.n_snapshots();
+  });
+}
+
+int dust2_gb300_unfilter_last_snapshots(dust2_gb300_unfilter* unfilter,
+                                        double* out) {
+  return guard([&] {
+    auto& u = unfref(unfilter);
+    need(out != nullptr, "out is NULL");
+    u.last_snapshots(out);
+  });
+}
+
 int dust2_gb300_unfilter_update_pars(dust2_gb300_unfilter* unfilter,
                                      const double* pars,
                                      const size_t* index_group,

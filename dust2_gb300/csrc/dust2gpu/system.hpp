@@ -161,6 +161,14 @@ template <class T>
 struct has_compare_data<T, std::void_t<decltype(&T::compare_data)>>
   : std::true_type {};
 
+// Adjoint support (sir.cpp:6 has_adjoint(): adjoint_update,
+// adjoint_compare_data, adjoint_initial and packing_gradient).
+template <class T, class = void>
+struct has_adjoint : std::false_type {};
+template <class T>
+struct has_adjoint<T, std::void_t<decltype(&T::adjoint_update)>>
+  : std::true_type {};
+
 template <class T, class = void>
 struct has_output : std::false_type {};
 template <class T>

@@ -170,6 +170,28 @@ public:
                    int n_index_group, double* ll_out) = 0;
   virtual void update_pars(const double* pars, const int* index_group,
                            int n_index_group) = 0;
+  // Gradient entries of the system (packing_gradient; 0 without adjoint
+  // support), and the adjoint run returning them with the likelihood.
+  virtual int n_gradient() const = 0;
+  virtual void run_adjoint(const double* initial, const int* index_group,
+                           int n_index_group, double* ll_out) = 0;
+  virtual void last_gradient(double* out) = 0;
+  virtual int n_last_gradient_groups() const = 0;
+  // Trajectories (state entries index_state, nullptr = all, at every data
+  // time) and snapshots (full state at the data times `obs`) of the
+  // following runs (unfilter.hpp:42-73 trajectories_.add); exports are
+  // [time][group][particle][entry] over the groups of the run that saved
+  // them, no reordering (r/unfilter.hpp:64-136).
+  virtual void set_save_trajectories(bool save, const int* index_state,
+                                     int n_index_state) = 0;
+  virtual void set_save_snapshots(const int* obs, int n_obs) = 0;
+  virtual bool trajectories_current() const = 0;
+  virtual bool snapshots_current() const = 0;
+  virtual int n_trajectory_state() const = 0;
+  virtual int n_snapshots() const = 0;
+  virtual const std::vector<int>& saved_groups() const = 0;
+  virtual void last_trajectories(double* out) = 0;
+  virtual void last_snapshots(double* out) = 0;
 };
 
 }  // namespace engine

@@ -343,11 +343,12 @@ public:
 
   // Launch a whole-run kernel of the unfilter (engine/unfilter.cuh) with
   // this system's solver record: kernel(view, ode view, control, time,
-  // times, n_times, requires_init, active, data, n_groups_data, ll).
-  template <typename K, typename D>
+  // times, n_times, requires_init, active, data, n_groups_data, ll,
+  // save) with `save` saying what to keep at each data time.
+  template <typename K, typename D, typename S>
   void launch_unfilter(const double* times_dev, int n_times,
                        const int* active, const D* data, int n_groups_data,
-                       double* ll, K kernel) {
+                       double* ll, K kernel, const S& save) {
     const auto& L = base_.layout();
     auto s = base_.stream();
     DUST2_CUDA(cudaMemcpyAsync(requires_init_dev_.data(),
@@ -356,7 +357,8 @@ public:
                                cudaMemcpyHostToDevice, s));
     kernel<<<base_.n_run_tiles(), L.tile_size, 0, s>>>(
       base_.run_view(), view_ode(), control_dev(), base_.time(), times_dev,
-      n_times, requires_init_dev_.data(), active, data, n_groups_data, ll);
+      n_times, requires_init_dev_.data(), active, data, n_groups_data, ll,
+      save);
     DUST2_CUDA(cudaGetLastError());
     std::fill(requires_initialise_.begin(), requires_initialise_.end(), 0);
   }

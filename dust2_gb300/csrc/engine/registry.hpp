@@ -59,6 +59,8 @@ std::string system_info_json() {
     << (is_continuous<T>() ? "continuous" : "discrete") << "\""
     << ", \"has_compare\": "
     << (has_compare_data<T>::value ? "true" : "false")
+    << ", \"has_adjoint\": "
+    << (has_adjoint<T>::value && !is_continuous<T>() ? "true" : "false")
     << ", \"n_state_max\": " << T::n_state_max;
   if constexpr (!is_continuous<T>()) {
     s << ", \"default_dt\": " << T::default_dt;

@@ -322,13 +322,16 @@ __global__ void k_export_snapshots(const double* snap_state,
       }
       --sn;
     }
-    j = hist_order[static_cast<long>(i) * stride + base + j];
+    if (hist_order != nullptr) {
+      j = hist_order[static_cast<long>(i) * stride + base + j];
+    }
   }
 }
 
 // trajectories.hpp:135-190 (export_state with reorder): one thread per
 // output particle walks back through the saved indices from the last data
-// time.  out: [time][group][particle][state].
+// time (hist_order null: no reordering, as for deterministic likelihoods).
+// out: [time][group][particle][state].
 __global__ void k_export_history(const double* hist_state,
                                  const int* hist_order, int n_times,
                                  int n_save, int stride,
@@ -350,7 +353,9 @@ __global__ void k_export_history(const double* hist_state,
     for (int s = 0; s < n_save; ++s) {
       dst[s] = hs[static_cast<long>(s) * stride + base + j];
     }
-    j = hist_order[static_cast<long>(i) * stride + base + j];
+    if (hist_order != nullptr) {
+      j = hist_order[static_cast<long>(i) * stride + base + j];
+    }
   }
 }
 

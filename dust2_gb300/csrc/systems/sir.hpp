@@ -27,6 +27,8 @@ struct sir {
 
   static constexpr int n_state_max = 5;
   static constexpr real_type default_dt = 1;
+  // state entries and the gradient of beta, gamma, I0 (sir.cpp:122-124)
+  static constexpr int n_adjoint_max = 8;
 
   // inst/examples/sir.cpp:7-11 (parameter annotations) and :74-81.
   static constexpr parameter_info parameters[] = {
@@ -61,6 +63,11 @@ struct sir {
 
   static int n_state(const shared_state&) {
     return 5;
+  }
+
+  // sir.cpp:122-124
+  static std::vector<packing_entry> packing_gradient(const shared_state&) {
+    return {{"beta", {}}, {"gamma", {}}, {"I0", {}}};
   }
 
   static zero_every_spec zero_every(const shared_state&) {
@@ -120,6 +127,73 @@ struct sir {
     const auto incidence_modelled = state[4];
     const auto lambda = incidence_modelled + noise;
     return density::poisson(incidence_observed, lambda, true);
+  }
+
+  // The adjoint equations of the deterministic model (sir.cpp:126-210),
+  // term for term: the reverse-mode derivatives of update, compare and
+  // initial with respect to state and to beta, gamma, I0.
+  DUST2_HD static void adjoint_initial(real_type time,
+                                       const real_type* state,
+                                       const real_type* adjoint,
+                                       const shared_state& shared,
+                                       internal_state& internal,
+                                       real_type* adjoint_next) {
+    const real_type adj_I = adjoint[1];
+    for (int i = 0; i < 7; ++i) {
+      adjoint_next[i] = adjoint[i];
+    }
+    adjoint_next[7] = adjoint[7] + adj_I;
+  }
+
+  DUST2_HD static void adjoint_update(real_type time, real_type dt,
+                                      const real_type* state,
+                                      const real_type* adjoint,
+                                      const shared_state& shared,
+                                      internal_state& internal,
+                                      real_type* adjoint_next) {
+    const auto S = state[0];
+    const auto I = state[1];
+    const auto adj_S = adjoint[0];
+    const auto adj_I = adjoint[1];
+    const auto adj_R = adjoint[2];
+    const auto adj_cases_cumul = adjoint[3];
+    const auto adj_cases_inc = adjoint[4];
+    const auto adj_beta = adjoint[5];
+    const auto adj_gamma = adjoint[6];
+    const auto adj_I0 = adjoint[7];
+    const auto p_SI = 1 - math::exp(-shared.beta * I / shared.N * dt);
+    const auto p_IR = 1 - math::exp(-shared.gamma * dt);
+    const auto adj_n_IR = -adj_I + adj_R;
+    const auto adj_n_SI = adj_cases_inc + adj_cases_cumul + adj_I + -adj_S;
+    const auto adj_p_IR = adj_n_IR * I;
+    const auto adj_p_SI = adj_n_SI * S;
+    const auto e_SI = math::exp(-shared.beta * I * dt / shared.N);
+    adjoint_next[0] = adj_n_SI * p_SI + adj_S;
+    adjoint_next[1] = adj_n_IR * p_IR +
+      adj_p_SI * (shared.beta * dt) * e_SI / shared.N + adj_I;
+    adjoint_next[2] = adj_R;
+    adjoint_next[3] = adj_cases_cumul;
+    adjoint_next[4] = adj_cases_inc;
+    adjoint_next[5] = adj_beta + adj_p_SI * I * dt * e_SI / shared.N;
+    adjoint_next[6] = adj_gamma + adj_p_IR * math::exp(-shared.gamma);
+    adjoint_next[7] = adj_I0;
+  }
+
+  DUST2_HD static void adjoint_compare_data(real_type time,
+                                            const real_type* state,
+                                            const real_type* adjoint,
+                                            const data_type& data,
+                                            const shared_state& shared,
+                                            internal_state& internal,
+                                            real_type* adjoint_next) {
+    const real_type cases_inc = state[4];
+    const real_type noise = 1 / shared.exp_noise;
+    const real_type lambda = cases_inc + noise;
+    const real_type adj_lambda = data.incidence / lambda - 1;
+    for (int i = 0; i < 8; ++i) {
+      adjoint_next[i] = adjoint[i];
+    }
+    adjoint_next[4] = adjoint[4] + adj_lambda;
   }
 };
 

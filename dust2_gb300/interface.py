@@ -33,6 +33,7 @@ class Generator:
         self.name = info["name"]
         self.time_type = info["time_type"]
         self.has_compare = info["has_compare"]
+        self.has_adjoint = info["has_adjoint"]
         self.parameters = info["parameters"]
         self.data_names = info["data"]
         self.default_dt = info.get("default_dt")
@@ -924,13 +925,16 @@ def _check_lik(obj):
 
 def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
                         index_state=None, index_group=None,
-                        save_snapshots=None):
-    """R/interface-likelihood.R:48-114, r/filter.hpp:112-143."""
+                        save_snapshots=None, adjoint=None):
+    """R/interface-likelihood.R:48-114, r/filter.hpp:112-143,
+    r/unfilter.hpp:20-62.  `adjoint` (unfilters; default: whether the
+    system has adjoint support) runs through the state history and makes
+    the gradient available to dust_likelihood_last_gradient."""
     _check_lik(obj)
-    if ((save_trajectories or save_snapshots is not None)
-            and isinstance(obj, DustUnfilter)):
-        raise DustError("save_trajectories is not supported for unfilters "
-                        "by this engine")
+    if adjoint is None:
+        adjoint = obj.generator.has_adjoint
+    elif not isinstance(adjoint, (bool, np.bool_)):
+        raise DustError("'adjoint' must be a scalar logical")
     snap_index = None
     if save_snapshots is not None:
         # R/interface-likelihood.R:83-92
@@ -980,12 +984,22 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
                                       obj.n_groups))
         init = as_f64(full.transpose(2, 1, 0))
     n_out = obj.n_groups if ig is None else ig.size
+    ist = None
+    if save_trajectories:
+        ist = _check_index(index_state, obj.n_state, "index_state")
     if isinstance(obj, DustUnfilter):
+        check(_lib.lib().dust2_gb300_unfilter_set_save_trajectories(
+            obj.ptr, 1 if save_trajectories else 0, sptr(ist),
+            0 if ist is None else ist.size))
+        check(_lib.lib().dust2_gb300_unfilter_set_save_snapshots(
+            obj.ptr, sptr(snap_index), 0 if snap_index is None else
+            snap_index.size))
         # r/unfilter.hpp:48-61: n_particles values per group
         ll = np.empty(n_out * obj.n_particles)
-        check(_lib.lib().dust2_gb300_unfilter_run(
-            obj.ptr, dptr(init), sptr(ig), 0 if ig is None else ig.size,
-            dptr(ll)))
+        run = (_lib.lib().dust2_gb300_unfilter_run_adjoint if adjoint else
+               _lib.lib().dust2_gb300_unfilter_run)
+        check(run(obj.ptr, dptr(init), sptr(ig),
+                  0 if ig is None else ig.size, dptr(ll)))
         ll = ll.reshape(n_out, obj.n_particles).T
         if obj.preserve_particle_dimension and obj.preserve_group_dimension:
             return ll
@@ -994,9 +1008,6 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
         if obj.preserve_group_dimension:
             return ll[0, :]
         return float(ll[0, 0])
-    ist = None
-    if save_trajectories:
-        ist = _check_index(index_state, obj.n_state, "index_state")
     check(_lib.lib().dust2_gb300_filter_set_save_trajectories(
         obj.ptr, 1 if save_trajectories else 0, sptr(ist),
         0 if ist is None else ist.size))
@@ -1012,12 +1023,74 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
     return ll
 
 
+def dust_likelihood_last_gradient(obj):
+    """R/interface-likelihood.R:309-331, r/unfilter.hpp:153-180: the
+    gradient of the last adjoint run's log-likelihood with respect to the
+    system's packing_gradient parameters (for sir: beta, gamma, I0),
+    shaped as the reference shapes it: a vector for one particle in one
+    group, (n_gradient, n_particles * n_groups) when one of the
+    dimensions is preserved, (n_gradient, n_particles, n_groups) when
+    both are."""
+    _check_lik(obj)
+    if obj.ptr is None:
+        raise DustError("Gradient is not current: likelihood has not yet "
+                        "been run")
+    if isinstance(obj, DustLikelihood):
+        raise DustError("Gradients need a deterministic likelihood "
+                        "(an unfilter)")
+    n_gr = ctypes.c_size_t()
+    n_grp = ctypes.c_size_t()
+    check(_lib.lib().dust2_gb300_unfilter_gradient_dim(
+        obj.ptr, ctypes.byref(n_gr), ctypes.byref(n_grp)))
+    if n_gr.value == 0:
+        raise DustError(f"The '{obj.generator.name}' system does not "
+                        "support adjoint methods")
+    if n_grp.value == 0:
+        raise DustError("System was not run with 'adjoint = TRUE'")
+    out = np.empty(n_gr.value * obj.n_particles * n_grp.value)
+    check(_lib.lib().dust2_gb300_unfilter_last_gradient(obj.ptr, dptr(out)))
+    pp, pg = obj.preserve_particle_dimension, obj.preserve_group_dimension
+    if pp and pg:
+        return out.reshape((n_gr.value, obj.n_particles, n_grp.value),
+                           order="F")
+    if pp or pg:
+        return out.reshape((n_gr.value, obj.n_particles * n_grp.value),
+                           order="F")
+    return out
+
+
+def _unfilter_saved(obj, what):
+    """r/unfilter.hpp:64-125: trajectories or snapshots of an unfilter
+    (no reordering, no particle selection), shaped (state, particle,
+    group, time) when both dimensions are preserved, (state, particle x
+    group, time) when one is, (state x particle x group, time) when
+    neither is."""
+    dims = [ctypes.c_size_t() for _ in range(4)]
+    dim_fn = getattr(_lib.lib(), f"dust2_gb300_unfilter_{what}_dim")
+    check(dim_fn(obj.ptr, *[ctypes.byref(x) for x in dims]))
+    n_state, n_particles, n_groups, n_time = [x.value for x in dims]
+    out = np.empty(n_state * n_particles * n_groups * n_time)
+    name = "trajectories" if what == "trajectory" else "snapshots"
+    check(getattr(_lib.lib(), f"dust2_gb300_unfilter_last_{name}")(
+        obj.ptr, dptr(out)))
+    pp, pg = obj.preserve_particle_dimension, obj.preserve_group_dimension
+    if pp and pg:
+        shape = (n_state, n_particles, n_groups, n_time)
+    elif pp or pg:
+        shape = (n_state, n_particles * n_groups, n_time)
+    else:
+        shape = (n_state * n_particles * n_groups, n_time)
+    return out.reshape(shape, order="F")
+
+
 def dust_likelihood_last_snapshots(obj, select_random_particle=False):
     """R/interface-likelihood.R:255-266, r/filter.hpp:98-137: array
     (state, particle, group, snapshot) with dust2's dimension dropping."""
     _check_lik(obj)
-    if obj.ptr is None or isinstance(obj, DustUnfilter):
+    if obj.ptr is None:
         raise DustError("Snapshots are not current")
+    if isinstance(obj, DustUnfilter):
+        return _unfilter_saved(obj, "snapshot")
     dims = [ctypes.c_size_t() for _ in range(4)]
     sel = 1 if select_random_particle else 0
     check(_lib.lib().dust2_gb300_filter_snapshot_dim(
@@ -1041,8 +1114,10 @@ def dust_likelihood_last_trajectories(obj, select_random_particle=False):
     r/filter.hpp:55-96: array (state, particle, group, time) with dust2's
     dimension dropping."""
     _check_lik(obj)
-    if obj.ptr is None or isinstance(obj, DustUnfilter):
+    if obj.ptr is None:
         raise DustError("Trajectories are not current")
+    if isinstance(obj, DustUnfilter):
+        return _unfilter_saved(obj, "trajectory")
     dims = [ctypes.c_size_t() for _ in range(4)]
     sel = 1 if select_random_particle else 0
     check(_lib.lib().dust2_gb300_filter_trajectory_dim(

@@ -23,6 +23,7 @@ import numpy as np
 
 from ._lib import DustError
 from .interface import (DustLikelihood, DustUnfilter,
+                        dust_likelihood_last_gradient,
                         dust_likelihood_last_state,
                         dust_likelihood_last_trajectories,
                         dust_likelihood_rng_state, dust_likelihood_run,
@@ -65,9 +66,11 @@ class DustModel:
     generator hand-off; `observe()` returns the observer's record."""
 
     def __init__(self, parameters, density, properties, get_rng_state=None,
-                 set_rng_state=None, observer=None, likelihood=None):
+                 set_rng_state=None, observer=None, likelihood=None,
+                 gradient=None):
         self.parameters = parameters
         self.density = density
+        self.gradient = gradient
         self.properties = properties
         self.get_rng_state = get_rng_state
         self.set_rng_state = set_rng_state
@@ -107,13 +110,27 @@ def dust_likelihood_monty(obj, packer, initial=None,
                                  save_trajectories=bool(save_trajectories))
         return float(np.sum(ll))
 
+    has_gradient = deterministic and obj.generator.has_adjoint
+    gradient = None
     if deterministic:
         def density(x):
             key = np.asarray(x, dtype=float).tobytes()
             if cache.get("key") != key:
                 cache["value"] = run(x)
                 cache["key"] = key
+                cache.pop("gradient", None)
             return cache["value"]
+
+        if has_gradient:
+            # R/monty.R:176-185: the gradient at x of the last adjoint run
+            # (the density runs with the adjoint by default), kept with the
+            # density until x changes
+            def gradient(x):
+                density(x)
+                if "gradient" not in cache:
+                    cache["gradient"] = np.ravel(
+                        dust_likelihood_last_gradient(obj))
+                return cache["gradient"]
     else:
         density = run
 
@@ -150,12 +167,12 @@ def dust_likelihood_monty(obj, packer, initial=None,
                 obj, rng_streams(_n_streams(obj), bytes(state)[:32]))
 
     properties = {"is_stochastic": not deterministic,
-                  "has_direct_sample": False, "has_gradient": False,
+                  "has_direct_sample": False, "has_gradient": has_gradient,
                   "allow_multiple_parameters": False,
                   "has_observer": observer is not None,
                   "has_parameter_groups": False}
     return DustModel(packer.names(), density, properties, get_rng_state,
-                     set_rng_state, observer, obj)
+                     set_rng_state, observer, obj, gradient)
 
 
 def served_model(server, session, packer, failure_is_impossible=False):

@@ -411,6 +411,75 @@ int dust2_gb300_unfilter_run(dust2_gb300_unfilter* unfilter,
                              const size_t* index_group,
                              size_t n_index_group, double* ll);
 
+/* dust2_unfilter_<sys>_run with adjoint = TRUE (r/unfilter.hpp:42-44,
+ * unfilter.hpp:77-110): the same log-likelihood as
+ * dust2_gb300_unfilter_run, through the saved state history, and the
+ * gradient of each particle's log-likelihood with respect to the
+ * system's packing_gradient parameters.  A system without adjoint support
+ * runs as dust2_gb300_unfilter_run and has no current gradient. */
+int dust2_gb300_unfilter_run_adjoint(dust2_gb300_unfilter* unfilter,
+                                     const double* initial,
+                                     const size_t* index_group,
+                                     size_t n_index_group, double* ll);
+
+/* Gradient length (packing_gradient; 0 without adjoint support) and the
+ * groups covered by the current gradient (0 when the last run was not an
+ * adjoint run). */
+int dust2_gb300_unfilter_gradient_dim(const dust2_gb300_unfilter* unfilter,
+                                      size_t* n_gradient,
+                                      size_t* n_groups_last);
+
+/* dust2_discrete_unfilter_last_gradient (r/unfilter.hpp:153-180,
+ * unfilter.hpp:135-142): n_gradient x n_particles x n_groups_last
+ * doubles, gradient entries fastest.  Fails with "System was not run with
+ * 'adjoint = TRUE'" after a plain run.  Unlike the reference, more than
+ * one particle per group is supported (each particle's own gradient). */
+int dust2_gb300_unfilter_last_gradient(dust2_gb300_unfilter* unfilter,
+                                       double* out);
+
+/* Save trajectories (state entries index_state, NULL = all) at every
+ * data time in the following runs (save_trajectories / index_state of
+ * dust2_unfilter_<sys>_run, r/unfilter.hpp:20-47, unfilter.hpp:60-62,
+ * 100-102). */
+int dust2_gb300_unfilter_set_save_trajectories(dust2_gb300_unfilter* unfilter,
+                                               int32_t save,
+                                               const size_t* index_state,
+                                               size_t n_index_state);
+
+/* Save the full state at the data times time_index (increasing; 0-based
+ * data-time positions) in the following runs (save_snapshots of
+ * dust2_unfilter_<sys>_run; trajectories.hpp:84-97).  Unlike the
+ * reference's plain run, snapshots are kept whether or not trajectories
+ * are. */
+int dust2_gb300_unfilter_set_save_snapshots(dust2_gb300_unfilter* unfilter,
+                                            const size_t* time_index,
+                                            size_t n);
+
+/* Shape of dust2_gb300_unfilter_last_trajectories: saved entries,
+ * particles per group, groups of the run that saved them, data times. */
+int dust2_gb300_unfilter_trajectory_dim(dust2_gb300_unfilter* unfilter,
+                                        size_t* n_state, size_t* n_particles,
+                                        size_t* n_groups, size_t* n_time);
+
+/* dust2_unfilter_<sys>_last_trajectories (r/unfilter.hpp:64-93): entries
+ * fastest, then particle, group, data time.  Fails with "Trajectories are
+ * not current" unless the last run saved them. */
+int dust2_gb300_unfilter_last_trajectories(dust2_gb300_unfilter* unfilter,
+                                           double* out);
+
+/* Shape of dust2_gb300_unfilter_last_snapshots: state entries, particles
+ * per group, groups, snapshots. */
+int dust2_gb300_unfilter_snapshot_dim(dust2_gb300_unfilter* unfilter,
+                                      size_t* n_state, size_t* n_particles,
+                                      size_t* n_groups,
+                                      size_t* n_snapshots);
+
+/* dust2_unfilter_<sys>_last_snapshots (r/unfilter.hpp:95-125); layout as
+ * dust2_gb300_unfilter_last_trajectories.  Fails with "Snapshots are not
+ * current" unless the last run saved them. */
+int dust2_gb300_unfilter_last_snapshots(dust2_gb300_unfilter* unfilter,
+                                        double* out);
+
 /* dust2_unfilter_<sys>_update_pars (r/unfilter.hpp:10-18). */
 int dust2_gb300_unfilter_update_pars(dust2_gb300_unfilter* unfilter,
                                      const double* pars,

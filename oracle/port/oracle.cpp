@@ -962,18 +962,129 @@ int oracle_filter_run(const char* name, const double* pars, int n_groups,
   }
 }
 
+// The adjoint run of a deterministic likelihood (unfilter.hpp:77-110 and
+// compute_gradient_, :188-229, with discrete/system.hpp:95-117, 425-481)
+// for the sir system, any number of particles per group: a forward pass
+// over all steps keeping the state after every step (before zero_every
+// resets, which act on the running copy), the compares at each data
+// time's saved state with the final system time, then the reverse
+// pass.  ll_out: [group][particle]; gradient_out:
+// [group][particle][n_gradient]; state_out: the state after the run.
+int oracle_unfilter_adjoint(const char* name, const double* pars,
+                            int n_groups, int n_particles, double time_start,
+                            const double* times, int n_times,
+                            const double* data, int n_groups_data, double dt,
+                            double* ll_out, double* gradient_out,
+                            double* state_out, char* err, int err_len) {
+  try {
+    const std::string nm(name);
+    if (nm != "sir") {
+      throw std::runtime_error("no adjoint for system " + nm);
+    }
+    using S = dust2gpu::systems::sir;
+    auto shared = shared_of<S>(pars, n_groups);
+    const int ns = S::n_state(shared[0]);
+    const int na = ns + 3;
+    std::vector<int> step_of(n_times);
+    for (int i = 0; i < n_times; ++i) {
+      step_of[i] = static_cast<int>(
+        std::round(std::max(0.0, times[i] - time_start) / dt));
+    }
+    const int n_steps = static_cast<int>(
+      std::round(std::max(0.0, times[n_times - 1] - time_start) / dt));
+    const double time_end = time_start + n_steps * dt;
+    std::vector<typename S::data_type> d;
+    for (int i = 0; i < n_times * n_groups_data; ++i) {
+      d.push_back(S::build_data(data + i));
+    }
+    for (int g = 0; g < n_groups; ++g) {
+      const auto z = zero_every_of<S>(shared[g]);
+      for (int j = 0; j < n_particles; ++j) {
+        const size_t k = static_cast<size_t>(g) * n_particles + j;
+        typename S::internal_state internal{};
+        rng_t rng{};
+        rng.deterministic = true;
+        std::vector<double> hist(static_cast<size_t>(n_steps + 1) * ns);
+        S::initial(time_start, shared[g], internal, rng, hist.data());
+        std::vector<double> x(hist.begin(), hist.begin() + ns);
+        for (int i = 0; i < n_steps; ++i) {
+          const double t = time_start + i * dt;
+          for (const auto& el : z) {
+            if (std::fmod(t, el.first) == 0) {
+              for (int s : el.second) {
+                x[s] = 0;
+              }
+            }
+          }
+          double* y = hist.data() + static_cast<size_t>(i + 1) * ns;
+          S::update(t, dt, x.data(), shared[g], internal, rng, y);
+          std::copy(y, y + ns, x.begin());
+        }
+        const auto& data_of = [&](int i) -> const typename S::data_type& {
+          return d[i * n_groups_data + (n_groups_data == 1 ? 0 : g)];
+        };
+        double acc = 0;
+        for (int i = 0; i < n_times; ++i) {
+          acc += S::compare_data(time_end, hist.data() + step_of[i] * ns,
+                                 data_of(i), shared[g], internal, rng);
+        }
+        std::vector<double> adj(na, 0.0), next(na, 0.0);
+        double time = time_end;
+        for (int i = n_times - 1; i >= 0; --i) {
+          const double time_i = i == 0 ? time_start : times[i - 1];
+          const double* st = hist.data() + static_cast<size_t>(step_of[i]) *
+            ns;
+          S::adjoint_compare_data(time, st, adj.data(), data_of(i),
+                                  shared[g], internal, next.data());
+          std::swap(adj, next);
+          const int n_back = static_cast<int>(
+            std::round(std::max(0.0, time - time_i) / dt));
+          for (int b = 1; b <= n_back; ++b) {
+            const double tb = time - b * dt;
+            S::adjoint_update(tb, dt, st - static_cast<size_t>(b) * ns,
+                              adj.data(), shared[g], internal, next.data());
+            std::swap(adj, next);
+            for (const auto& el : z) {
+              if (std::fmod(tb, el.first) == 0) {
+                for (int s : el.second) {
+                  adj[s] = 0;
+                }
+              }
+            }
+          }
+          time = time_i;
+        }
+        S::adjoint_initial(time, hist.data(), adj.data(), shared[g],
+                           internal, next.data());
+        ll_out[k] = acc;
+        std::copy(next.begin() + ns, next.end(), gradient_out + k * 3);
+        std::copy(x.begin(), x.end(), state_out + k * ns);
+      }
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
 // dust2::unfilter (unfilter.hpp:42-73, reset :162-186) on a deterministic
 // system: initial conditions, then for each data time run_to_time and
 // compare_data, summing per particle.  ll_out: [n_runs][group][particle];
 // state_out (optional): the state after the last run.
-int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
-                        int n_particles, double time_start,
-                        const double* times, int n_times, const double* data,
-                        int n_groups_data, double dt, int max_steps,
-                        double atol, double rtol, double step_size_min,
-                        double step_size_max, int n_runs, double* ll_out,
-                        double* state_out, int n_threads, char* err,
-                        int err_len) {
+// states_out (oracle_unfilter_states; may be null): the full state of the
+// last run at every data time, [time][group][particle][state], as
+// trajectories and snapshots record it (unfilter.hpp:60-62).
+static int unfilter_run_impl(const char* name, const double* pars,
+                             int n_groups, int n_particles,
+                             double time_start, const double* times,
+                             int n_times, const double* data,
+                             int n_groups_data, double dt, int max_steps,
+                             double atol, double rtol, double step_size_min,
+                             double step_size_max, int n_runs,
+                             double* ll_out, double* state_out,
+                             double* states_out, int n_threads, char* err,
+                             int err_len) {
   try {
     const size_t n_total = static_cast<size_t>(n_groups) * n_particles;
     const std::string nm(name);
@@ -1016,6 +1127,10 @@ int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
                 t, y.data(), d[i * n_groups_data + (n_groups_data == 1 ? 0 :
                                                     g)],
                 shared[g], internal, rng);
+              if (states_out != nullptr && r == n_runs - 1) {
+                std::copy(y.begin(), y.end(), states_out +
+                          (static_cast<size_t>(i) * n_total + k) * n_state);
+              }
             }
           } catch (const std::exception& e) {
             err_k.e[k].code = std::string(e.what()) == "too many steps" ?
@@ -1058,6 +1173,10 @@ int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
             for (size_t k = 0; k < n_total; ++k) {
               ll[k] += step[k];
             }
+            if (states_out != nullptr && r == n_runs - 1) {
+              std::copy(sys.state.begin(), sys.state.end(), states_out +
+                        static_cast<size_t>(i) * sys.state.size());
+            }
           }
         }
         if (state_out != nullptr) {
@@ -1075,6 +1194,36 @@ int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
     set_err(err, err_len, e.what());
     return 1;
   }
+}
+
+int oracle_unfilter_run(const char* name, const double* pars, int n_groups,
+                        int n_particles, double time_start,
+                        const double* times, int n_times, const double* data,
+                        int n_groups_data, double dt, int max_steps,
+                        double atol, double rtol, double step_size_min,
+                        double step_size_max, int n_runs, double* ll_out,
+                        double* state_out, int n_threads, char* err,
+                        int err_len) {
+  return unfilter_run_impl(name, pars, n_groups, n_particles, time_start,
+                           times, n_times, data, n_groups_data, dt,
+                           max_steps, atol, rtol, step_size_min,
+                           step_size_max, n_runs, ll_out, state_out, nullptr,
+                           n_threads, err, err_len);
+}
+
+int oracle_unfilter_states(const char* name, const double* pars,
+                           int n_groups, int n_particles, double time_start,
+                           const double* times, int n_times,
+                           const double* data, int n_groups_data, double dt,
+                           int max_steps, double atol, double rtol,
+                           double step_size_min, double step_size_max,
+                           double* ll_out, double* states_out, char* err,
+                           int err_len) {
+  return unfilter_run_impl(name, pars, n_groups, n_particles, time_start,
+                           times, n_times, data, n_groups_data, dt,
+                           max_steps, atol, rtol, step_size_min,
+                           step_size_max, 1, ll_out, nullptr, states_out, 1,
+                           err, err_len);
 }
 
 // One filter run saving trajectories of state entries index_state (all

@@ -188,6 +188,92 @@ class Oracle:
         self._call(self._unf, *args)
         return ll.reshape(n_runs, n_groups, n_particles), state
 
+    def unfilter_states(self, name, pars, n_groups, n_particles, time_start,
+                        times, data, n_groups_data, n_state, dt=1.0,
+                        max_steps=10000, atol=1e-6, rtol=1e-6,
+                        step_size_min=np.finfo(float).eps,
+                        step_size_max=np.inf):
+        """(port) One deterministic likelihood run returning (ll [group]
+        [particle], the full state at every data time [time][group]
+        [particle][state])."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        n_total = n_groups * n_particles
+        ll = np.empty(n_total)
+        states = np.empty(times.size * n_total * n_state)
+        self._call(self.lib.oracle_unfilter_states, _c(name.encode()),
+                   _dp(pars), _n(n_groups), _n(n_particles),
+                   ctypes.c_double(time_start), _dp(times), _n(times.size),
+                   _dp(data), _n(n_groups_data), ctypes.c_double(dt),
+                   _n(max_steps), ctypes.c_double(atol),
+                   ctypes.c_double(rtol), ctypes.c_double(step_size_min),
+                   ctypes.c_double(step_size_max), _dp(ll), _dp(states))
+        return (ll.reshape(n_groups, n_particles),
+                states.reshape(times.size, n_groups, n_particles, n_state))
+
+    def unfilter_trajectories(self, name, pars, n_groups, n_particles,
+                              time_start, times, data, n_groups_data, dt,
+                              n_state, index_state=None, snapshots=None,
+                              adjoint=False):
+        """(reference) One unfilter run (run_adjoint when `adjoint`)
+        saving trajectories of index_state (None = all) and snapshots at
+        the data times `snapshots`; returns (ll [group][particle],
+        trajectories [time][group][particle][entry], snapshots
+        [snapshot][group][particle][state])."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        ist = (np.zeros(0, dtype=np.int32) if index_state is None else
+               np.ascontiguousarray(index_state, dtype=np.int32))
+        n_save = n_state if index_state is None else ist.size
+        snaps = (np.zeros(0) if snapshots is None else
+                 np.ascontiguousarray(snapshots, dtype=np.float64))
+        n_total = n_groups * n_particles
+        ll = np.empty(n_total)
+        traj = np.empty(times.size * n_total * n_save)
+        snap = np.empty(max(1, snaps.size * n_total * n_state))
+        ip = ctypes.POINTER(ctypes.c_int)
+        self._call(self.lib.ref_unfilter_trajectories, _c(name.encode()),
+                   _dp(pars), _n(n_groups), _n(n_particles),
+                   ctypes.c_double(time_start), _dp(times), _n(times.size),
+                   _dp(data), _n(n_groups_data), ctypes.c_double(dt),
+                   ist.ctypes.data_as(ip), _n(ist.size), _dp(snaps),
+                   _n(snaps.size), _n(1 if adjoint else 0), _dp(ll),
+                   _dp(traj), _dp(snap))
+        return (ll.reshape(n_groups, n_particles),
+                traj.reshape(times.size, n_groups, n_particles, n_save),
+                snap[:snaps.size * n_total * n_state].reshape(
+                    snaps.size, n_groups, n_particles, n_state))
+
+    def unfilter_adjoint(self, name, pars, n_groups, n_particles,
+                         time_start, times, data, n_groups_data, n_state,
+                         dt=1.0, n_gradient=3):
+        """One adjoint run of a deterministic likelihood and its gradient
+        (unfilter::run_adjoint + last_gradient); returns (ll [group]
+        [particle], gradient [group][particle][n_gradient], state).  The
+        reference build takes one particle per group."""
+        if self.kind == "ref" and n_particles != 1:
+            raise OracleError("the reference computes gradients for one "
+                              "particle per group")
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        n_total = n_groups * n_particles
+        ll = np.empty(n_total)
+        gr = np.empty(n_total * n_gradient)
+        state = np.empty(n_total * n_state)
+        fn = getattr(self.lib, self.prefix + "unfilter_adjoint")
+        args = [_c(name.encode()), _dp(pars), _n(n_groups)]
+        if self.kind == "port":
+            args.append(_n(n_particles))
+        args += [ctypes.c_double(time_start), _dp(times), _n(times.size),
+                 _dp(data), _n(n_groups_data), ctypes.c_double(dt), _dp(ll),
+                 _dp(gr), _dp(state)]
+        self._call(fn, *args)
+        return (ll.reshape(n_groups, n_particles),
+                gr.reshape(n_groups, n_particles, n_gradient), state)
+
     def filter_trajectories(self, name, pars, n_groups, n_particles,
                             time_start, times, data, n_groups_data, dt, rng,
                             n_state_saved, index_state=None, select=None,

@@ -15,6 +15,7 @@
 // reference engine expects to catch (discrete/system.hpp:82-84).
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -98,6 +99,53 @@ struct ref_discrete {
   static dust2::zero_every_type<real_type> zero_every(
       const shared_state& shared) {
     return zero_every_of<S>(shared);
+  }
+};
+
+// The same system with its adjoint methods forwarded, so that
+// dust2::properties sees packing_gradient (properties.hpp:19-21, 121-129)
+// and unfilter::last_gradient runs compute_gradient_.
+template <typename S>
+struct ref_discrete_adjoint : ref_discrete<S> {
+  using real_type = double;
+  using shared_state = typename S::shared_state;
+  using internal_state = typename S::internal_state;
+  using data_type = typename S::data_type;
+
+  // dust2::packing is built from an initializer list only; the systems
+  // with adjoints here have three scalar gradient entries.
+  static dust2::packing packing_gradient(const shared_state& shared) {
+    const auto e = S::packing_gradient(shared);
+    if (e.size() != 3 || !e[0].dims.empty() || !e[1].dims.empty() ||
+        !e[2].dims.empty()) {
+      throw std::runtime_error("expected three scalar gradient entries");
+    }
+    return dust2::packing{{e[0].name, {}}, {e[1].name, {}}, {e[2].name, {}}};
+  }
+  static void adjoint_initial(real_type time, const real_type* state,
+                              const real_type* adjoint,
+                              const shared_state& shared,
+                              internal_state& internal,
+                              real_type* adjoint_next) {
+    S::adjoint_initial(time, state, adjoint, shared, internal, adjoint_next);
+  }
+  static void adjoint_update(real_type time, real_type dt,
+                             const real_type* state,
+                             const real_type* adjoint,
+                             const shared_state& shared,
+                             internal_state& internal,
+                             real_type* adjoint_next) {
+    S::adjoint_update(time, dt, state, adjoint, shared, internal,
+                      adjoint_next);
+  }
+  static void adjoint_compare_data(real_type time, const real_type* state,
+                                   const real_type* adjoint,
+                                   const data_type& data,
+                                   const shared_state& shared,
+                                   internal_state& internal,
+                                   real_type* adjoint_next) {
+    S::adjoint_compare_data(time, state, adjoint, data, shared, internal,
+                            adjoint_next);
   }
 };
 
@@ -513,12 +561,18 @@ int ref_unfilter_run(const char* name, const double* pars, int n_groups,
       const auto& st = obj.sys.state();
       std::copy(st.begin(), st.end(), state_out);
     };
+    // one data entry per group and time (r/helpers.hpp:406-424); shared
+    // data is repeated for each group
     auto data_of = [&](auto s) {
       using S = typename decltype(s)::type;
       std::vector<typename S::data_type> d;
       const int nd = sizeof(typename S::data_type) / sizeof(double);
-      for (int i = 0; i < n_times * n_groups_data; ++i) {
-        d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+      for (int i = 0; i < n_times; ++i) {
+        for (int g = 0; g < n_groups; ++g) {
+          const int gd = n_groups_data == 1 ? 0 : g;
+          d.push_back(S::build_data(
+            data + (static_cast<size_t>(i) * n_groups_data + gd) * nd));
+        }
       }
       return d;
     };
@@ -555,6 +609,137 @@ int ref_unfilter_run(const char* name, const double* pars, int n_groups,
     if (!ok) {
       throw std::runtime_error("unknown system " + nm);
     }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// One unfilter run (run, or run_adjoint when adjoint != 0) saving
+// trajectories of the entries index_state (n_index_state 0 = all) and
+// snapshots at the data times `snapshots` (unfilter.hpp:42-110), then the
+// exports of r/unfilter.hpp:64-125 (no reordering).  traj_out:
+// [time][group][particle][entry]; snap_out: [snapshot][group][particle]
+// [state]; ll_out: [group][particle].
+int ref_unfilter_trajectories(const char* name, const double* pars,
+                              int n_groups, int n_particles,
+                              double time_start, const double* times,
+                              int n_times, const double* data,
+                              int n_groups_data, double dt,
+                              const int* index_state, int n_index_state,
+                              const double* snapshots, int n_snapshots,
+                              int adjoint, double* ll_out, double* traj_out,
+                              double* snap_out, char* err, int err_len) {
+  try {
+    std::vector<double> tt(times, times + n_times);
+    std::vector<uint64_t> seed{42};
+    std::vector<size_t> is(index_state, index_state + n_index_state);
+    std::vector<double> snaps(snapshots, snapshots + n_snapshots);
+    auto finish = [&](auto& obj, bool use_adjoint) {
+      if (use_adjoint) {
+        obj.run_adjoint(true, true, snaps, is, obj.sys.all_groups());
+      } else {
+        obj.run(true, true, snaps, is, obj.sys.all_groups());
+      }
+      const auto& ll = obj.last_log_likelihood();
+      std::copy(ll.begin(), ll.end(), ll_out);
+      const auto& tr = obj.last_trajectories();
+      tr.export_state(traj_out, false, {});
+      if (n_snapshots > 0) {
+        tr.export_snapshots(snap_out, false, {});
+      }
+    };
+    auto data_of = [&](auto s) {
+      using S = typename decltype(s)::type;
+      std::vector<typename S::data_type> d;
+      const int nd = sizeof(typename S::data_type) / sizeof(double);
+      for (int i = 0; i < n_times; ++i) {
+        for (int g = 0; g < n_groups; ++g) {
+          const int gd = n_groups_data == 1 ? 0 : g;
+          d.push_back(S::build_data(
+            data + (static_cast<size_t>(i) * n_groups_data + gd) * nd));
+        }
+      }
+      return d;
+    };
+    const std::string nm(name);
+    if (nm == "sirode") {
+      using S = dust2gpu::systems::sirode;
+      using T = ref_continuous<S>;
+      auto shared = shared_of<S>(pars, n_groups);
+      std::vector<typename T::internal_state> internal(n_groups);
+      dust2::ode::control<double> ctl(10000, 1e-6, 1e-6,
+                                      std::numeric_limits<double>::epsilon(),
+                                      std::numeric_limits<double>::infinity(),
+                                      {}, false, false);
+      dust2::dust_continuous<T> sys(shared, internal, time_start, 0, ctl,
+                                    n_particles, seed, true, 1);
+      dust2::unfilter<dust2::dust_continuous<T>> obj(sys, time_start, tt,
+                                                     data_of(tag<S>{}));
+      finish(obj, false);
+      return 0;
+    }
+    if (nm != "sir") {
+      throw std::runtime_error("unsupported system " + nm);
+    }
+    using S = dust2gpu::systems::sir;
+    using T = ref_discrete_adjoint<S>;
+    auto shared = shared_of<S>(pars, n_groups);
+    std::vector<typename T::internal_state> internal(n_groups);
+    dust2::dust_discrete<T> sys(shared, internal, time_start, dt, n_particles,
+                                seed, true, 1);
+    dust2::unfilter<dust2::dust_discrete<T>> obj(sys, time_start, tt,
+                                                 data_of(tag<S>{}));
+    finish(obj, adjoint != 0);
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// unfilter::run_adjoint then last_gradient (unfilter.hpp:77-110,
+// 135-142, 188-229) for the sir system, seeded 42, n_particles 1 per
+// group; ll_out: [group]; gradient_out: [group][n_gradient]; state_out:
+// the state after the run.  The reference copies gradients correctly for
+// one particle per group only (adjoint_data.hpp:75-83).
+int ref_unfilter_adjoint(const char* name, const double* pars, int n_groups,
+                         double time_start, const double* times, int n_times,
+                         const double* data, int n_groups_data, double dt,
+                         double* ll_out, double* gradient_out,
+                         double* state_out, char* err, int err_len) {
+  try {
+    const std::string nm(name);
+    if (nm != "sir") {
+      throw std::runtime_error("no adjoint for system " + nm);
+    }
+    using S = dust2gpu::systems::sir;
+    using T = ref_discrete_adjoint<S>;
+    std::vector<double> tt(times, times + n_times);
+    std::vector<uint64_t> seed{42};
+    auto shared = shared_of<S>(pars, n_groups);
+    std::vector<typename T::internal_state> internal(n_groups);
+    dust2::dust_discrete<T> sys(shared, internal, time_start, dt, 1, seed,
+                                true, 1);
+    // The reference holds one data entry per group and time
+    // (r/helpers.hpp:406-424); shared data is repeated for each group.
+    std::vector<typename S::data_type> d;
+    const int nd = sizeof(typename S::data_type) / sizeof(double);
+    for (int i = 0; i < n_times; ++i) {
+      for (int g = 0; g < n_groups; ++g) {
+        const int gd = n_groups_data == 1 ? 0 : g;
+        d.push_back(S::build_data(
+          data + (static_cast<size_t>(i) * n_groups_data + gd) * nd));
+      }
+    }
+    dust2::unfilter<dust2::dust_discrete<T>> obj(sys, time_start, tt, d);
+    obj.run_adjoint(true, false, {}, {}, obj.sys.all_groups());
+    const auto& ll = obj.last_log_likelihood();
+    std::copy(ll.begin(), ll.end(), ll_out);
+    obj.last_gradient(gradient_out);
+    const auto& st = obj.sys.state();
+    std::copy(st.begin(), st.end(), state_out);
     return 0;
   } catch (const std::exception& e) {
     set_err(err, err_len, e.what());

@@ -9,7 +9,8 @@ numpy implementation in tests/xoshiro.py, so the fixtures do not depend
 on the engine under test.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(`--unfilter` / `--trajectories` write only those fixtures).
+(`--unfilter` / `--trajectories` / `--adjoint` /
+`--unfilter-trajectories` write only those fixtures).
 """
 
 import sys
@@ -142,6 +143,8 @@ def main():
          lw_w1=w1, lw_w2=w2, lw_w3=w3)
     unfilters(ref)
     trajectories(ref)
+    adjoints(ref)
+    unfilter_trajectories(ref)
 
 
 def unfilters(ref):
@@ -196,8 +199,77 @@ def trajectories(ref):
          snapshots=snapshots, snap=snap, snap_one=snap_one)
 
 
+ADJOINT_CASES = [
+    # (label, groups' parameters, time_start, times, dt, n_groups_data)
+    ("four_days", [{}], 0.0, [4.0, 8, 12, 16], 1.0, 1),
+    ("odd_steps", [{}], 0.0, [3.0, 6, 9, 12], 1.0, 1),
+    ("four_groups", [{"beta": 0.1 * (i + 1)} for i in range(4)], 0.0,
+     [4.0, 8, 12, 16], 1.0, 4),
+    ("quarter_days", [{"beta": 0.3, "gamma": 0.1}], 0.0,
+     [float(t) for t in range(1, 21)], 0.25, 1),
+    ("late_start", [{"beta": 0.25}, {"beta": 0.15, "I0": 30}], 2.0,
+     [5.0, 9, 10, 15], 0.5, 1),
+]
+
+
+def adjoints(ref):
+    """10. Gradients of deterministic likelihoods (unfilter::run_adjoint +
+    last_gradient, test-unfilter-adjoint.R): the sir system, one particle
+    per group (the reference copies gradients for one particle only),
+    beta/gamma/N/I0/exp_noise = 0.1/0.2/1000/10/1e6 unless a case
+    changes them; incidence 1, 2, ... per group and time."""
+    out = {}
+    for label, groups, t0, times, dt, ngd in ADJOINT_CASES:
+        base = {"beta": 0.1, "gamma": 0.2, "N": 1000, "I0": 10,
+                "exp_noise": 1e6}
+        pars = workload_data.sir_pars([dict(base, **g) for g in groups])
+        times = np.array(times)
+        data = np.arange(1, times.size * ngd + 1, dtype=float)
+        ll, gr, state = ref.unfilter_adjoint("sir", pars, len(groups), 1,
+                                             t0, times, data, ngd, 5, dt=dt)
+        for k, v in [("pars", pars), ("times", times), ("data", data),
+                     ("ll", ll), ("gradient", gr), ("state", state),
+                     ("meta", np.array([len(groups), t0, dt, ngd]))]:
+            out[f"{label}__{k}"] = v
+    save("adjoint_sir", labels=np.array([c[0] for c in ADJOINT_CASES]),
+         **out)
+
+
+def unfilter_trajectories(ref):
+    """11. Deterministic likelihood trajectories and snapshots
+    (unfilter.hpp:42-110 trajectories_.add, r/unfilter.hpp:64-125,
+    test-unfilter.R / test-unfilter-adjoint.R "can save trajectories"):
+    the unfilter_sir inputs (2 groups x 3 particles, dt = 0.25) with all
+    state and entries 1, 3 (0-based), snapshots at times 8 and 20, through
+    run and run_adjoint; the sirode inputs (2 x 2) with a snapshot at
+    12."""
+    g = np.load(OUT / "unfilter_sir.npz")
+    times, data, pars = g["times"], g["data"], g["pars"]
+    snaps = np.array([8.0, 20.0])
+    ll, full, snap = ref.unfilter_trajectories(
+        "sir", pars, 2, 3, 0.0, times, data, 2, 0.25, 5, snapshots=snaps)
+    _, sub, _ = ref.unfilter_trajectories(
+        "sir", pars, 2, 3, 0.0, times, data, 2, 0.25, 5, index_state=[1, 3])
+    ll_a, full_a, snap_a = ref.unfilter_trajectories(
+        "sir", pars, 2, 3, 0.0, times, data, 2, 0.25, 5, snapshots=snaps,
+        adjoint=True)
+    g = np.load(OUT / "unfilter_sirode.npz")
+    ode_snaps = np.array([12.0])
+    ll_o, full_o, snap_o = ref.unfilter_trajectories(
+        "sirode", g["pars"], 2, 2, 0.0, g["times"], g["data"], 2, 0.0, 5,
+        snapshots=ode_snaps)
+    save("unfilter_trajectories", snapshots=snaps, ll=ll, full=full,
+         snap=snap, sub=sub, ll_adjoint=ll_a, full_adjoint=full_a,
+         snap_adjoint=snap_a, ode_snapshots=ode_snaps, ll_ode=ll_o,
+         full_ode=full_o, snap_ode=snap_o)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--unfilter"]:
+    if sys.argv[1:] == ["--adjoint"]:
+        adjoints(pyoracle.ref())
+    elif sys.argv[1:] == ["--unfilter-trajectories"]:
+        unfilter_trajectories(pyoracle.ref())
+    elif sys.argv[1:] == ["--unfilter"]:
         unfilters(pyoracle.ref())
     elif sys.argv[1:] == ["--trajectories"]:
         trajectories(pyoracle.ref())

@@ -102,3 +102,77 @@ def test_unfilter_matches_port_on_many_groups(built, port):
     want, _ = port.unfilter_run("sirode", w["pars"], 300, 1, 0.0, times,
                                 data.ravel(), 300, 5)
     np.testing.assert_allclose(ll, want[0][:, 0], rtol=1e-10, atol=0)
+
+
+def _from_reference(a):
+    """[time][group][particle][entry] -> (entry, particle, group, time)."""
+    return np.transpose(a, (3, 2, 1, 0))
+
+
+@pytest.mark.parametrize("adjoint", [False, True])
+def test_unfilter_trajectories_match_reference(built, adjoint):
+    t = golden("unfilter_trajectories")
+    g = golden("unfilter_sir")
+    gen = d.sir()
+    obj = d.dust_unfilter_create(gen, 0, columns(g), n_particles=3, dt=0.25)
+    pars = plist(gen, g["pars"])
+    with pytest.raises(d.DustError, match="Trajectories are not current"):
+        d.dust_likelihood_last_trajectories(obj)
+    ll = d.dust_likelihood_run(obj, pars, save_trajectories=True,
+                               save_snapshots=t["snapshots"],
+                               adjoint=adjoint)
+    np.testing.assert_array_equal(ll.T, t["ll"])
+    tr = d.dust_likelihood_last_trajectories(obj)
+    assert tr.shape == (5, 3, 2, g["times"].size)
+    np.testing.assert_array_equal(tr, _from_reference(t["full"]))
+    sn = d.dust_likelihood_last_snapshots(obj)
+    assert sn.shape == (5, 3, 2, 2)
+    np.testing.assert_array_equal(sn, _from_reference(t["snap"]))
+    # index_state is 1-based, as in R: entries 1 and 3 counted from 0
+    d.dust_likelihood_run(obj, pars, save_trajectories=True,
+                          index_state=[2, 4], adjoint=adjoint)
+    np.testing.assert_array_equal(d.dust_likelihood_last_trajectories(obj),
+                                  _from_reference(t["sub"]))
+    with pytest.raises(d.DustError, match="Snapshots are not current"):
+        d.dust_likelihood_last_snapshots(obj)
+    d.dust_likelihood_run(obj, pars, adjoint=adjoint)
+    with pytest.raises(d.DustError, match="Trajectories are not current"):
+        d.dust_likelihood_last_trajectories(obj)
+
+
+def test_unfilter_ode_trajectories_match_reference(built):
+    t = golden("unfilter_trajectories")
+    g = golden("unfilter_sirode")
+    gen = d.sirode()
+    obj = d.dust_unfilter_create(gen, 0, columns(g), n_particles=2)
+    pars = plist(gen, g["pars"])
+    ll = d.dust_likelihood_run(obj, pars, save_trajectories=True,
+                               save_snapshots=t["ode_snapshots"])
+    np.testing.assert_allclose(ll.T, t["ll_ode"], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(d.dust_likelihood_last_trajectories(obj),
+                               _from_reference(t["full_ode"]), rtol=1e-9,
+                               atol=1e-9)
+    np.testing.assert_allclose(d.dust_likelihood_last_snapshots(obj),
+                               _from_reference(t["snap_ode"]), rtol=1e-9,
+                               atol=1e-9)
+
+
+def test_unfilter_trajectories_shapes_and_groups(built):
+    """r/unfilter.hpp:84-90 dimension dropping, and trajectories of the
+    groups the run covered."""
+    t = golden("unfilter_trajectories")
+    g = golden("unfilter_sir")
+    gen = d.sir()
+    pars = plist(gen, g["pars"])
+    obj = d.dust_unfilter_create(gen, 0, columns(g), dt=0.25)
+    d.dust_likelihood_run(obj, pars, save_trajectories=True)
+    tr = d.dust_likelihood_last_trajectories(obj)
+    # one particle per group: groups kept, particles folded in
+    assert tr.shape == (5, 2, g["times"].size)
+    full = _from_reference(t["full"])
+    np.testing.assert_array_equal(tr, full[:, 0, :, :])
+    d.dust_likelihood_run(obj, None, save_trajectories=True,
+                          index_group=[2])
+    tr = d.dust_likelihood_last_trajectories(obj)
+    assert tr.shape == (5, 1, g["times"].size)
+    np.testing.assert_array_equal(tr[:, 0, :], full[:, 0, 1, :])

@@ -70,6 +70,31 @@ def test_deterministic_density_is_cached(built):
     assert model.density([0.3]) != v
 
 
+def test_unfilter_model_has_gradient(built):
+    # R/monty.R:129: deterministic likelihoods of systems with adjoints
+    obj = d.dust_unfilter_create(d.sir(), 0, sir_data())
+    model = monty.dust_likelihood_monty(obj, monty.Packer(["beta"]))
+    assert model.properties["has_gradient"]
+    obj = d.dust_unfilter_create(d.sirode(), 0, sir_data())
+    model = monty.dust_likelihood_monty(obj, monty.Packer(["beta"]))
+    assert not model.properties["has_gradient"] and model.gradient is None
+
+
+@pytest.mark.gpu
+def test_model_gradient_is_the_last_gradient(built):
+    data = sir_data()
+    fixed = {"N": 1000, "I0": 10, "exp_noise": 1e6}
+    packer = monty.Packer(["beta", "gamma"], fixed=fixed)
+    a = d.dust_unfilter_create(d.sir(), 0, data)
+    b = d.dust_unfilter_create(d.sir(), 0, data)
+    model = monty.dust_likelihood_monty(a, packer)
+    for x in ([0.2, 0.1], [0.3, 0.1]):
+        want_ll = d.dust_likelihood_run(b, packer.unpack(x), adjoint=True)
+        want = d.dust_likelihood_last_gradient(b)
+        np.testing.assert_array_equal(model.gradient(x), want)
+        assert model.density(x) == want_ll
+
+
 @pytest.mark.gpu
 def test_served_chains_equal_plain_chains(built):
     gen = d.sir()

@@ -9,6 +9,7 @@ checked against the golden fixtures that engine produced
 import numpy as np
 import pytest
 
+import dust2_gb300
 import xoshiro
 import workload_data
 from conftest import golden
@@ -197,6 +198,114 @@ def test_port_unfilter_equals_reference_engine(port, name):
                                   n_runs=2, n_threads=2)
     np.testing.assert_array_equal(ll, g["ll"])
     np.testing.assert_array_equal(state, g["state"])
+
+
+ADJOINT_LABELS = ["four_days", "odd_steps", "four_groups", "quarter_days",
+                  "late_start"]
+
+
+def _adjoint_case(g, label):
+    n_groups, t0, dt, ngd = g[f"{label}__meta"]
+    return (g[f"{label}__pars"], int(n_groups), float(t0),
+            g[f"{label}__times"], g[f"{label}__data"], int(ngd), float(dt))
+
+
+@pytest.mark.parametrize("label", ADJOINT_LABELS)
+def test_port_adjoint_equals_reference_engine(port, label):
+    g = golden("adjoint_sir")
+    pars, G, t0, times, data, ngd, dt = _adjoint_case(g, label)
+    ll, gr, state = port.unfilter_adjoint("sir", pars, G, 1, t0, times,
+                                          data, ngd, 5, dt=dt)
+    np.testing.assert_array_equal(ll, g[f"{label}__ll"])
+    np.testing.assert_array_equal(gr, g[f"{label}__gradient"])
+    np.testing.assert_array_equal(state, g[f"{label}__state"])
+    # the adjoint run's log-likelihood is the plain run's
+    ll_plain, _ = port.unfilter_run("sir", pars, G, 1, t0, times, data, ngd,
+                                    5, dt=dt)
+    np.testing.assert_array_equal(ll_plain[0], ll)
+
+
+def test_reference_adjoint_reproduces_fixture(ref):
+    g = golden("adjoint_sir")
+    for label in ADJOINT_LABELS:
+        pars, G, t0, times, data, ngd, dt = _adjoint_case(g, label)
+        ll, gr, _ = ref.unfilter_adjoint("sir", pars, G, 1, t0, times, data,
+                                         ngd, 5, dt=dt)
+        np.testing.assert_array_equal(ll, g[f"{label}__ll"])
+        np.testing.assert_array_equal(gr, g[f"{label}__gradient"])
+
+
+@pytest.mark.parametrize("label", ["four_days", "odd_steps"])
+def test_adjoint_gradient_matches_finite_differences(port, label):
+    """test-unfilter-adjoint.R "can run the adjoint model": the gradient
+    in (beta, gamma, I0) against central differences of the plain
+    likelihood, compared as R's all.equal does (sum of absolute
+    differences over sum of absolute values) to 1e-4.  At dt = 1 the
+    model's adjoint is exact in beta and gamma; its I0 entry leaves out
+    the S = N - I0 dependence, which this tolerance allows, as in the
+    reference's own test."""
+    g = golden("adjoint_sir")
+    pars, G, t0, times, data, ngd, dt = _adjoint_case(g, label)
+    names = [p["name"] for p in dust2_gb300.sir().parameters]
+    idx = [names.index(n) for n in ("beta", "gamma", "I0")]
+    _, gr, _ = port.unfilter_adjoint("sir", pars, G, 1, t0, times, data,
+                                     ngd, 5, dt=dt)
+
+    def f(x):
+        p = np.array(pars, dtype=float)
+        p[idx] = x
+        ll, _ = port.unfilter_run("sir", p, 1, 1, t0, times, data, ngd, 5,
+                                  dt=dt)
+        return ll.ravel()[0]
+
+    x0 = np.asarray(pars, dtype=float)[idx]
+    num = np.empty(3)
+    for i in range(3):
+        h = 1e-5 * max(1.0, abs(x0[i]))
+        e = np.zeros(3)
+        e[i] = h
+        num[i] = (f(x0 + e) - f(x0 - e)) / (2 * h)
+    got = gr.ravel()
+    assert np.sum(np.abs(num - got)) / np.sum(np.abs(num)) < 1e-4
+    np.testing.assert_allclose(got[:2], num[:2], rtol=1e-6)
+
+
+def test_port_adjoint_particles_agree(port):
+    """Several particles per group (the engine's extension): each carries
+    the one-particle gradient of its group."""
+    g = golden("adjoint_sir")
+    pars, G, t0, times, data, ngd, dt = _adjoint_case(g, "four_groups")
+    ll1, gr1, _ = port.unfilter_adjoint("sir", pars, G, 1, t0, times, data,
+                                        ngd, 5, dt=dt)
+    ll5, gr5, _ = port.unfilter_adjoint("sir", pars, G, 5, t0, times, data,
+                                        ngd, 5, dt=dt)
+    np.testing.assert_array_equal(ll5, np.repeat(ll1, 5, axis=1))
+    np.testing.assert_array_equal(gr5, np.repeat(gr1, 5, axis=1))
+
+
+def test_port_unfilter_states_equal_reference_trajectories(port):
+    """The deterministic run's state at each data time is what dust2's
+    unfilter saves as trajectories and snapshots (run and run_adjoint
+    alike)."""
+    t = golden("unfilter_trajectories")
+    g = golden("unfilter_sir")
+    ll, states = port.unfilter_states("sir", g["pars"], 2, 3, 0.0,
+                                      g["times"], g["data"], 2, 5, dt=0.25)
+    np.testing.assert_array_equal(ll, t["ll"])
+    np.testing.assert_array_equal(states, t["full"])
+    np.testing.assert_array_equal(states[..., [1, 3]], t["sub"])
+    snap_at = np.searchsorted(g["times"], t["snapshots"])
+    np.testing.assert_array_equal(states[snap_at], t["snap"])
+    np.testing.assert_array_equal(t["full_adjoint"], t["full"])
+    np.testing.assert_array_equal(t["snap_adjoint"], t["snap"])
+    np.testing.assert_array_equal(t["ll_adjoint"], t["ll"])
+    g = golden("unfilter_sirode")
+    ll, states = port.unfilter_states("sirode", g["pars"], 2, 2, 0.0,
+                                      g["times"], g["data"], 2, 5)
+    np.testing.assert_array_equal(ll, t["ll_ode"])
+    np.testing.assert_array_equal(states, t["full_ode"])
+    snap_at = np.searchsorted(g["times"], t["ode_snapshots"])
+    np.testing.assert_array_equal(states[snap_at], t["snap_ode"])
 
 
 def test_port_trajectories_equal_reference_engine(port):
