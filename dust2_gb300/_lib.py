@@ -94,6 +94,11 @@ _SIGNATURES = {
         ctypes.c_double, c_double_p, ctypes.c_size_t, c_double_p,
         ctypes.c_size_t, ctypes.c_double, c_u64_p, ctypes.c_size_t,
         c_void_pp]),
+    "dust2_gb300_filter_alloc_continuous": (ctypes.c_int, [
+        ctypes.c_char_p, c_double_p, ctypes.c_size_t, ctypes.c_size_t,
+        ctypes.c_double, c_double_p, ctypes.c_size_t, c_double_p,
+        ctypes.c_size_t, ctypes.c_double, ctypes.POINTER(OdeControl),
+        c_u64_p, ctypes.c_size_t, c_void_pp]),
     "dust2_gb300_filter_alloc_uneven": (ctypes.c_int, [
         ctypes.c_char_p, c_double_p, ctypes.c_size_t, c_size_p,
         ctypes.c_double, c_double_p, ctypes.c_size_t, c_double_p,

@@ -584,13 +584,21 @@ static int filter_alloc_impl(const char* name, const double* pars,
                              double time_start, const double* time,
                              size_t n_time, const double* data,
                              size_t n_groups_data, double dt,
+                             const dust2_gb300_ode_control* control,
                              const uint64_t* seed, size_t seed_len,
                              dust2_gb300_filter** out) {
   return guard([&] {
     need(out != nullptr, "out is NULL");
     need(n_groups >= 1, "'n_groups' must be at least 1");
     need(n_time >= 1, "Expected 'data' to have at least one row");
-    need(dt > 0, "Expected 'dt' to be greater than 0");
+    // discrete systems need dt > 0; a mixed-time system may run without
+    // updates (dt = 0, check_dt(allow_null = TRUE), R/filter-support.R)
+    const auto* f0 = dust2gpu::engine::find_system(name);
+    if (control == nullptr || !f0->continuous) {
+      need(dt > 0, "Expected 'dt' to be greater than 0");
+    } else {
+      need(dt >= 0, "Expected 'dt' to be greater than 0");
+    }
     need(n_groups_data == 1 || n_groups_data == n_groups,
          "Expected 'data' to have 1 or n_groups groups");
     // r/helpers.hpp check_time_sequence(require_later = true)
@@ -613,10 +621,11 @@ static int filter_alloc_impl(const char* name, const double* pars,
       n_streams += static_cast<std::size_t>(n) + 2;
     }
     auto words = seed_streams(seed, seed_len, n_streams);
+    const auto ctl = to_control(control);
     auto* impl = f->create_filter(pars, static_cast<int>(n_groups), np,
                                   time_start, time, static_cast<int>(n_time),
                                   data, static_cast<int>(n_groups_data), dt,
-                                  words, 0);
+                                  ctl, words, 0);
     *out = new dust2_gb300_filter{std::unique_ptr<filter_api>(impl), {}};
   });
 }
@@ -630,7 +639,8 @@ int dust2_gb300_filter_alloc(const char* name, const double* pars,
                              dust2_gb300_filter** out) {
   std::vector<int> np(n_groups, static_cast<int>(n_particles));
   return filter_alloc_impl(name, pars, n_groups, np, time_start, time, n_time,
-                           data, n_groups_data, dt, seed, seed_len, out);
+                           data, n_groups_data, dt, nullptr, seed, seed_len,
+                           out);
 }
 
 int dust2_gb300_filter_alloc_uneven(const char* name, const double* pars,
@@ -646,7 +656,24 @@ int dust2_gb300_filter_alloc_uneven(const char* name, const double* pars,
     np.push_back(static_cast<int>(n_particles[g]));
   }
   return filter_alloc_impl(name, pars, n_groups, np, time_start, time, n_time,
-                           data, n_groups_data, dt, seed, seed_len, out);
+                           data, n_groups_data, dt, nullptr, seed, seed_len,
+                           out);
+}
+
+int dust2_gb300_filter_alloc_continuous(
+    const char* name, const double* pars, size_t n_groups,
+    size_t n_particles, double time_start, const double* time, size_t n_time,
+    const double* data, size_t n_groups_data, double dt,
+    const dust2_gb300_ode_control* control, const uint64_t* seed,
+    size_t seed_len, dust2_gb300_filter** out) {
+  std::vector<int> np(n_groups, static_cast<int>(n_particles));
+  static const dust2_gb300_ode_control defaults{
+    10000, 1e-6, 1e-6, 0, std::numeric_limits<double>::infinity(), nullptr,
+    0, 0};
+  return filter_alloc_impl(name, pars, n_groups, np, time_start, time, n_time,
+                           data, n_groups_data, dt,
+                           control == nullptr ? &defaults : control, seed,
+                           seed_len, out);
 }
 
 int dust2_gb300_filter_free(dust2_gb300_filter* filter) {

@@ -380,6 +380,26 @@ DUST2_HD double negative_binomial_mu(double x, double size, double mu,
   return log ? ret : math::exp(ret);
 }
 
+// x log y with 0 log 0 = 0.
+DUST2_HD double x_log_y(double x, double y) {
+  return (x == 0 && y == 0) ? 0 : x * math::log(y);
+}
+
+// log Binomial(x | size, prob): log C(size, x) + x log p
+// + (size - x) log(1 - p), with 0 log 0 = 0 (so p = 0 or 1 give 0 or -Inf
+// without special cases).
+DUST2_HD double binomial(double x, double size, double prob, bool log) {
+  double ret;
+  if (x == 0 && size == 0) {
+    ret = 0;
+  } else {
+    ret = math::lgamma(size + 1.0) - math::lgamma(x + 1.0) -
+      math::lgamma(size - x + 1.0) + x_log_y(x, prob) +
+      x_log_y(size - x, 1 - prob);
+  }
+  return log ? ret : math::exp(ret);
+}
+
 DUST2_HD double normal(double x, double mu, double sd, bool log) {
   const double z = (x - mu) / sd;
   const double ret = -0.5 * z * z - math::log(sd) - math::HALF_LOG_2PI;

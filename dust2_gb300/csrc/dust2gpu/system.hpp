@@ -189,6 +189,32 @@ constexpr bool is_continuous() {
   return has_rhs<T>::value;
 }
 
+// Mixed time: an ODE (rhs) with a discrete-time update applied every dt
+// (properties.hpp:99 is_mixed_time, continuous/system.hpp:544-585).
+template <typename T>
+constexpr bool is_mixed_time() {
+  return has_rhs<T>::value && has_update<T>::value;
+}
+
+// "Special" state: entries after the ODE variables (and before any
+// outputs) that the rhs reads but the solver does not integrate; only the
+// update changes them (properties.hpp:130-153 size_special,
+// do_n_state_special; malaria.cpp's beta).
+template <class T, class = void>
+struct has_special : std::false_type {};
+template <class T>
+struct has_special<T, std::void_t<decltype(T::n_special)>>
+  : std::true_type {};
+
+template <typename T>
+constexpr int n_special() {
+  if constexpr (has_special<T>::value) {
+    return T::n_special;
+  } else {
+    return 0;
+  }
+}
+
 // Static checks every system must pass before the engine accepts it.
 template <typename T>
 constexpr bool check_system() {
@@ -198,8 +224,9 @@ constexpr bool check_system() {
                 "internal_state must be trivially copyable");
   static_assert(std::is_trivially_copyable<typename T::data_type>::value,
                 "data_type must be trivially copyable");
-  static_assert(has_rhs<T>::value != has_update<T>::value,
-                "a system has either update (discrete) or rhs (continuous)");
+  static_assert(has_rhs<T>::value || has_update<T>::value,
+                "a system has update (discrete), rhs (continuous) or both "
+                "(mixed time)");
   return true;
 }
 

@@ -117,12 +117,72 @@ __device__ __forceinline__ void refresh_output(
   }
 }
 
+// Advance one particle from t to t_end.  Pure ODE systems (and mixed-time
+// systems run without a dt) integrate with the solver.  Mixed-time
+// systems with dt > 0 follow run_to_time1 (continuous/system.hpp:544-585)
+// exactly: n_steps = (t_end - t) / dt truncated (none when t_end - t <
+// dt, and then nothing happens); step s integrates from where the last one
+// ended to t + s dt, the last step to t_end, so the first step is empty
+// and, with several steps, the last spans two intervals; after each, the
+// update runs at time t_end on a copy of the rest of the state and with a
+// copy of the particle's generator (update_ takes it by value, :408-416,
+// so the stream never advances); when the update changed the state the
+// solver is re-initialised at t.  Returns the generator's error code from
+// an update, or 0.
+template <typename T, int NV>
+__device__ __forceinline__ int advance(
+    dopri5::solver<T, NV>& sol, double t, double t_end, double dt, double* y,
+    const zero_every_spec& zero, dopri5::state<NV>& st,
+    dopri5::scratch<NV>& s, const random::rng_state& rng,
+    const typename T::shared_state& shared,
+    typename T::internal_state& internal) {
+  if constexpr (is_mixed_time<T>()) {
+    if (dt > 0) {
+      if (!(t_end > t)) {
+        return 0;
+      }
+      const long n_steps = static_cast<long>((t_end - t) / dt);
+      const int n_variables = sol.n_var + sol.n_special;
+      double y_other[T::n_state_max];
+      double t1 = t;
+      for (long step = 0; step < n_steps && st.err == 0; ++step) {
+        const double t0 = t1;
+        t1 = (step == n_steps - 1) ? t_end :
+          t + static_cast<double>(step) * dt;
+        sol.run(t0, t1, y, zero, st, s);
+        if (st.err != 0) {
+          break;
+        }
+        for (int i = 0; i < n_variables; ++i) {
+          y_other[i] = y[i];
+        }
+        random::rng_state r = rng;
+        T::update(t_end, dt, y, shared, internal, r, y_other);
+        if (r.err != 0) {
+          return r.err;
+        }
+        bool changed = false;
+        for (int i = 0; i < n_variables; ++i) {
+          changed = changed || !(y_other[i] == y[i]);
+          y[i] = y_other[i];
+        }
+        if (changed) {
+          sol.initialise(t, y, st, s);
+        }
+      }
+      return 0;
+    }
+  }
+  sol.run(t, t_end, y, zero, st, s);
+  return 0;
+}
+
 // Integrate every particle through `times` (n_times >= 1), writing the
 // state at each time to out[(i * n_total + k) * n_out + j] (j over
 // index_out, or over all state when index_out is null) when out is set.
 template <typename T>
 __global__ void k_ode_run(system_view<T> v, ode_view o,
-                          dopri5::control_dev ctl, double time0,
+                          dopri5::control_dev ctl, double time0, double dt,
                           const double* times, int n_times,
                           const int* requires_init, int n_total,
                           double* out, const int* index_out, int n_out) {
@@ -141,22 +201,26 @@ __global__ void k_ode_run(system_view<T> v, ode_view o,
   const int g = group_of(v, tl, k);
   const auto& shared = mixed ? v.shared[g] : sm.shared();
   const zero_every_spec& zero = mixed ? v.zero_every[g] : sm.zero;
-  const int n_var = v.n_state - T::n_output;
+  const int n_var = v.n_state - T::n_output - n_special<T>();
   typename T::internal_state internal{};
   double y[T::n_state_max];
   load_state<T>(v, k, y);
+  const auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
+  int update_err = 0;
   dopri5::state<NV> st;
   dopri5::scratch<NV> s;
   load_ode<NV>(o, k, n_var, st);
   dopri5::solver<T, NV> sol{ctl, shared, internal, n_var, k};
+  sol.n_special = n_special<T>();
   if (requires_init[g]) {
     sol.initialise(time0, y, st, s);
   }
   double t = time0;
   for (int i = 0; i < n_times; ++i) {
     const double t_end = times[i];
-    if (st.err == 0) {
-      sol.run(t, t_end, y, zero, st, s);
+    if (st.err == 0 && update_err == 0) {
+      update_err = advance<T, NV>(sol, t, t_end, dt, y, zero, st, s, rng,
+                                  shared, internal);
     }
     t = t_end;
     if (out != nullptr) {
@@ -176,9 +240,9 @@ __global__ void k_ode_run(system_view<T> v, ode_view o,
   refresh_output<T>(t, y, shared, internal);
   store_state<T>(v, k, y);
   store_ode<NV>(o, k, n_var, st);
-  if (st.err != 0) {
+  if (st.err != 0 || update_err != 0) {
     random::rng_state r{};
-    r.err = st.err;
+    r.err = st.err != 0 ? st.err : update_err;
     capture_error(v.errors, v.any_error, k, r);
   }
 }
@@ -213,14 +277,16 @@ public:
   static constexpr int NV = n_var_max<T>();
   static_assert(check_system<T>(), "invalid system");
 
+  // dt: the update interval of a mixed-time system (0: no updates; always
+  // 0 for a pure ODE).
   continuous_system(std::vector<shared_state> shared, double time,
                     const ode_control& control,
                     const std::vector<int>& n_particles,
                     const std::vector<std::uint64_t>& rng_words,
-                    bool deterministic, int tile_size = 0) :
+                    bool deterministic, int tile_size = 0, double dt = 0) :
     base_(std::move(shared), time, 0.0, n_particles, rng_words,
           deterministic, tile_size > 0 ? tile_size : 128),
-    control_(control),
+    control_(control), dt_(dt),
     requires_initialise_(base_.n_groups(), 1) {
     const auto& L = base_.layout();
     const std::size_t S = L.stride;
@@ -278,7 +344,7 @@ public:
     return base_.time();
   }
   double dt() const override {
-    return 0;
+    return dt_;
   }
   bool errors_pending() const override {
     return base_.errors_pending();
@@ -343,7 +409,7 @@ public:
 
   // Launch a whole-run kernel of the unfilter (engine/unfilter.cuh) with
   // this system's solver record: kernel(view, ode view, control, time,
-  // times, n_times, requires_init, active, data, n_groups_data, ll,
+  // dt, times, n_times, requires_init, active, data, n_groups_data, ll,
   // save) with `save` saying what to keep at each data time.
   template <typename K, typename D, typename S>
   void launch_unfilter(const double* times_dev, int n_times,
@@ -356,9 +422,9 @@ public:
                                requires_initialise_.size() * sizeof(int),
                                cudaMemcpyHostToDevice, s));
     kernel<<<base_.n_run_tiles(), L.tile_size, 0, s>>>(
-      base_.run_view(), view_ode(), control_dev(), base_.time(), times_dev,
-      n_times, requires_init_dev_.data(), active, data, n_groups_data, ll,
-      save);
+      base_.run_view(), view_ode(), control_dev(), base_.time(), dt_,
+      times_dev, n_times, requires_init_dev_.data(), active, data,
+      n_groups_data, ll, save);
     DUST2_CUDA(cudaGetLastError());
     std::fill(requires_initialise_.begin(), requires_initialise_.end(), 0);
   }
@@ -495,7 +561,6 @@ public:
 
   static constexpr int step_times_cap = 4096;
 
-private:
   dopri5::control_dev control_dev() {
     dopri5::control_dev c;
     c.max_steps = control_.max_steps;
@@ -525,6 +590,42 @@ private:
                     base_.layout().stride};
   }
 
+  // Enqueue the reordering of every particle's solver record on stream s
+  // (continuous/system.hpp:199-203, ode_internals moved with the state);
+  // arguments as k_reorder's.
+  void enqueue_reorder_record(const tile* tiles, int n_tiles, int tile_size,
+                              const int* group_offset, const int* index,
+                              const int* group_mode, cudaStream_t s) {
+    const int S = base_.layout().stride;
+    auto move = [&](double* a, int n_rows) {
+      k_reorder<<<n_tiles, tile_size, 0, s>>>(a, other_.data(), S, n_rows,
+                                              tiles, group_offset, index,
+                                              group_mode);
+      DUST2_CUDA(cudaMemcpyAsync(a, other_.data(),
+                                 static_cast<std::size_t>(n_rows) * S *
+                                 sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
+    };
+    move(dydt_.data(), NV);
+    move(c_.data(), 5 * NV);
+    move(t0_.data(), 1);
+    move(t1_.data(), 1);
+    move(h_.data(), 1);
+    move(step_size_.data(), 1);
+    move(error_.data(), 1);
+    int* tmp = reinterpret_cast<int*>(other_.data());
+    for (int* a : {n_steps_.data(), n_acc_.data(), n_rej_.data()}) {
+      k_reorder_int<<<n_tiles, tile_size, 0, s>>>(a, tmp, S, tiles,
+                                                  group_offset, index,
+                                                  group_mode);
+      DUST2_CUDA(cudaMemcpyAsync(a, tmp, static_cast<std::size_t>(S) *
+                                 sizeof(int), cudaMemcpyDeviceToDevice, s));
+    }
+    DUST2_CUDA(cudaGetLastError());
+  }
+
+private:
+
   void launch_run(const double* times, int n_times, double* out_dev,
                   const int* index_dev, int n_out) {
     const auto& L = base_.layout();
@@ -540,7 +641,7 @@ private:
                                requires_initialise_.size() * sizeof(int),
                                cudaMemcpyHostToDevice, s));
     k_ode_run<T><<<base_.n_run_tiles(), L.tile_size, 0, s>>>(
-      base_.run_view(), view_ode(), control_dev(), base_.time(),
+      base_.run_view(), view_ode(), control_dev(), base_.time(), dt_,
       times_dev_.data(), n_times, requires_init_dev_.data(), L.n_total,
       out_dev, index_dev, n_out);
     DUST2_CUDA(cudaGetLastError());
@@ -580,6 +681,7 @@ private:
   // errors and the state verbs; this class adds the solver record.
   discrete_system<T> base_;
   ode_control control_;
+  double dt_ = 0;
   std::vector<int> requires_initialise_;
   device_array<double> dydt_, c_, t0_, t1_, h_, step_size_, error_;
   device_array<int> n_steps_, n_acc_, n_rej_;

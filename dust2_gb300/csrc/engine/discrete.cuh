@@ -515,7 +515,7 @@ public:
   }
 
   void launch_run(double t0, int n_steps) {
-    if constexpr (has_update<T>::value) {
+    if constexpr (has_update<T>::value && !dust2gpu::is_continuous<T>()) {
       if (n_steps > 0) {
         k_run<T><<<n_run_tiles(), layout_.tile_size, 0, stream_>>>(
           run_view(), t0, dt_, n_steps);

@@ -139,6 +139,18 @@ struct solver {
   typename T::internal_state& internal;
   int n_var;
   int particle;
+  // Special state after the n_var integrated variables: read by the rhs,
+  // carried unchanged through every stage (solver.hpp:236-239, 274-276).
+  int n_special = 0;
+
+  DUST2_HD void copy_special(const double* y, double* dst) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      if (i >= n_var && i < n_var + n_special) {
+        dst[i] = y[i];
+      }
+    }
+  }
 
   DUST2_HD void rhs(double t, const double* y, double* dydt) {
     T::rhs(t, y, shared, internal, dydt);
@@ -391,6 +403,10 @@ struct solver {
   DUST2_HD double run(double t, double t_end, double* y,
                       const zero_every_spec& z, state<NV>& st,
                       scratch<NV>& s) {
+    if (n_special > 0) {
+      copy_special(y, s.y_next);
+      copy_special(y, s.y_stiff);
+    }
     if (ctl.n_critical == 0) {
       while (t < t_end && st.err == 0) {
         apply_zero_every(t, y, z, st);
@@ -435,6 +451,9 @@ struct solver {
     double* f0 = st.dydt;
     double* f1 = s.k3;
     double* y1 = s.y_next;
+    if (n_special > 0) {
+      copy_special(y, y1);
+    }
     rhs(t, y, f0);
     double norm_f = 0.0;
     double norm_y = 0.0;

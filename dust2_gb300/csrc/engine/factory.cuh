@@ -52,12 +52,34 @@ system_api* create_system(const double* pars, int n_groups,
   bind_lf_table();
   auto shared = build_shared_groups<T>(pars, n_groups);
   if constexpr (is_continuous<T>()) {
+    // dt is the update interval of a mixed-time system (0: none)
     return new continuous_system<T>(std::move(shared), time, control,
                                     n_particles, rng_words, deterministic,
-                                    tile_size);
+                                    tile_size, is_mixed_time<T>() ? dt : 0);
   } else {
     return new discrete_system<T>(std::move(shared), time, dt, n_particles,
                                   rng_words, deterministic, tile_size);
+  }
+}
+
+// The system under a filter: discrete, or mixed time (r/continuous/
+// filter.hpp builds a dust_continuous with the dt of the time control).
+template <typename T>
+auto make_filter_system(std::vector<typename T::shared_state> shared,
+                        double time_start, double dt,
+                        const ode_control& control,
+                        const std::vector<int>& n_particles,
+                        const std::vector<std::uint64_t>& words,
+                        int tile_size) {
+  if constexpr (is_continuous<T>()) {
+    return std::make_unique<continuous_system<T>>(
+      std::move(shared), time_start, control, n_particles, words, false,
+      tile_size, dt);
+  } else {
+    (void)control;
+    return std::make_unique<discrete_system<T>>(
+      std::move(shared), time_start, dt, n_particles, words, false,
+      tile_size);
   }
 }
 
@@ -66,9 +88,12 @@ filter_api* create_filter(const double* pars, int n_groups,
                           const std::vector<int>& n_particles,
                           double time_start, const double* times, int n_times,
                           const double* data, int n_groups_data, double dt,
+                          const ode_control& control,
                           const std::vector<std::uint64_t>& rng_words,
                           int tile_size) {
-  if constexpr (is_continuous<T>() || !has_compare_data<T>::value) {
+  if constexpr ((is_continuous<T>() && !is_mixed_time<T>()) ||
+                !has_compare_data<T>::value) {
+    // R/interface-filter.R:59-65 refuses pure continuous-time systems
     throw std::runtime_error(
       is_continuous<T>() ?
       "Can't use 'dust_filter_create()' with continuous-time models" :
@@ -87,9 +112,9 @@ filter_api* create_filter(const double* pars, int n_groups,
         sys_words.push_back(rng_words[pos++]);
       }
     }
-    auto sys = std::make_unique<discrete_system<T>>(
-      std::move(shared), time_start, dt, n_particles, sys_words, false,
-      tile_size);
+    auto sys = make_filter_system<T>(std::move(shared), time_start, dt,
+                                     control, n_particles, sys_words,
+                                     tile_size);
     const int nd = sys->n_data();
     std::vector<typename T::data_type> d;
     d.reserve(static_cast<std::size_t>(n_times) * n_groups_data);
@@ -144,7 +169,8 @@ unfilter_api* create_unfilter(const double* pars, int n_groups,
     std::vector<double> t(times, times + n_times);
     if constexpr (is_continuous<T>()) {
       auto sys = std::make_unique<continuous_system<T>>(
-        std::move(shared), time_start, control, n_particles, words, true);
+        std::move(shared), time_start, control, n_particles, words, true, 0,
+        is_mixed_time<T>() ? dt : 0);
       return new unfilter_engine<T>(std::move(sys), time_start, std::move(t),
                                     std::move(d), n_groups_data);
     } else {

@@ -53,6 +53,7 @@
 #include "../dust2gpu/math.hpp"
 #include "../dust2gpu/random.hpp"
 #include "api.hpp"
+#include "continuous.cuh"
 #include "device.cuh"
 #include "discrete.cuh"
 #include "kernels_common.cuh"
@@ -161,6 +162,71 @@ __device__ __forceinline__ void step_compare_tile(
   }
 }
 
+// k_step_compare for mixed-time systems (filter.hpp:59-60 over
+// dust_continuous): each particle integrates from time0 to the data time
+// with its solver record (initialised first when `initialise` is set, at
+// the first data time of a run), applying updates every dt (see
+// advance()), and compares its state as it stands, outputs not refreshed
+// (continuous/system.hpp:279-305).  The group reductions are
+// k_step_compare's.
+template <typename T>
+DUST2_PARTICLE_KERNEL(T) k_step_compare_mixed(
+    system_view<T> v, ode_view o, dopri5::control_dev ctl, filter_view f,
+    double time0, double time, double dt, int initialise,
+    const typename T::data_type* data, int n_groups_data) {
+  constexpr int NV = n_var_max<T>();
+  __shared__ shared_smem<T> sm;
+  __shared__ double red[33];
+  const tile tl = v.tiles[blockIdx.x];
+  if (!f.active[tl.group]) {
+    return;
+  }
+  sm.load(v, tl.group);
+  __syncthreads();
+  const bool valid = static_cast<int>(threadIdx.x) < tl.count;
+  double logw = 0;
+  if (valid) {
+    const int k = tl.start + threadIdx.x;
+    const auto& shared = sm.shared();
+    auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
+    typename T::internal_state internal{};
+    const int n_var = v.n_state - T::n_output - n_special<T>();
+    double y[T::n_state_max];
+    load_state<T>(v, k, y);
+    dopri5::state<NV> st;
+    dopri5::scratch<NV> s;
+    load_ode<NV>(o, k, n_var, st);
+    dopri5::solver<T, NV> sol{ctl, shared, internal, n_var, k};
+    sol.n_special = n_special<T>();
+    if (initialise) {
+      sol.initialise(time0, y, st, s);
+    }
+    int update_err = 0;
+    if (st.err == 0) {
+      update_err = advance<T, NV>(sol, time0, time, dt, y, sm.zero, st, s,
+                                  rng, shared, internal);
+    }
+    const auto& d = data[n_groups_data == 1 ? 0 : tl.group];
+    logw = T::compare_data(time, y, d, shared, internal, rng);
+    store_state<T>(v, k, y);
+    store_ode<NV>(o, k, n_var, st);
+    if (st.err != 0 || update_err != 0) {
+      rng.err = st.err != 0 ? st.err : update_err;
+    }
+    capture_error(v.errors, v.any_error, k, rng);
+    f.w[k] = logw;
+  }
+  const int nz = __syncthreads_or(valid && logw != 0);
+  const double mx = block_max(valid && !(logw != logw) ? logw : -INFINITY,
+                              red);
+  if (threadIdx.x == 0) {
+    if (nz) {
+      atomicOr(f.gnz + tl.group, 1);
+    }
+    atomicMax(f.gkey + tl.group, ordered_key(mx));
+  }
+}
+
 template <typename T>
 DUST2_PARTICLE_KERNEL(T) k_step_compare(system_view<T> v, filter_view f,
                                         double time,
@@ -234,25 +300,36 @@ template <typename T>
 class filter_engine : public filter_api {
 public:
   using data_type = typename T::data_type;
+  // Discrete-time systems, or mixed-time ones (an ODE with updates; the
+  // filter of r/continuous/filter.hpp over dust_continuous).
+  using system_type = std::conditional_t<is_continuous<T>(),
+                                         continuous_system<T>,
+                                         discrete_system<T>>;
 
   // data: [n_times][n_groups_data] data_type; rng_words: the full stream
   // block of the filter, per group [2 filter | n_g particle] streams.
-  filter_engine(std::unique_ptr<discrete_system<T>> sys, double time_start,
+  filter_engine(std::unique_ptr<system_type> sys, double time_start,
                 std::vector<double> times, std::vector<data_type> data,
                 int n_groups_data, const std::vector<std::uint64_t>& rng_words) :
-    sys_(std::move(sys)), time_start_(time_start), times_(std::move(times)),
-    n_groups_data_(n_groups_data) {
+    owner_(std::move(sys)), sys_(&base_of(*owner_)), time_start_(time_start),
+    times_(std::move(times)), n_groups_data_(n_groups_data) {
     const auto& L = sys_->layout();
     const int G = L.n_groups;
     const int N = L.n_total;
     const int NT = L.n_tiles();
-    // schedule
+    // schedule: discrete systems step to the data times
+    // (discrete/system.hpp:62); continuous ones run to them exactly
     double t = time_start_;
     for (double ti : times_) {
-      const int n = static_cast<int>(
-        std::round(std::max(0.0, ti - t) / sys_->dt()));
-      schedule_.push_back(obs_step{t, n, t + n * sys_->dt()});
-      t = t + n * sys_->dt();
+      if constexpr (is_continuous<T>()) {
+        schedule_.push_back(obs_step{t, 0, ti});
+        t = ti;
+      } else {
+        const int n = static_cast<int>(
+          std::round(std::max(0.0, ti - t) / sys_->dt()));
+        schedule_.push_back(obs_step{t, n, t + n * sys_->dt()});
+        t = t + n * sys_->dt();
+      }
     }
     active_.resize(G);
     n_part_.resize(G);
@@ -298,7 +375,7 @@ public:
   }
 
   system_api& sys() override {
-    return *sys_;
+    return *owner_;
   }
   discrete_system<T>& system() {
     return *sys_;
@@ -637,7 +714,7 @@ public:
 
   void update_pars(const double* pars, const int* index_group,
                    int n_index_group) override {
-    sys_->update_pars(pars, index_group, n_index_group);
+    owner_->update_pars(pars, index_group, n_index_group);
   }
 
   std::size_t n_rng_streams() const override {
@@ -766,9 +843,16 @@ private:
       if (timing_) {
         record(ev_step_[2 * i]);
       }
-      k_step_compare<T><<<NT, TS, 0, s>>>(
-        v, f, st.t0, S.dt(), st.n_steps, st.t_compare,
-        data_.data() + i * n_groups_data_, n_groups_data_);
+      if constexpr (is_continuous<T>()) {
+        k_step_compare_mixed<T><<<NT, TS, 0, s>>>(
+          v, owner_->view_ode(), owner_->control_dev(), f, st.t0,
+          st.t_compare, owner_->dt(), i == 0 ? 1 : 0,
+          data_.data() + i * n_groups_data_, n_groups_data_);
+      } else {
+        k_step_compare<T><<<NT, TS, 0, s>>>(
+          v, f, st.t0, S.dt(), st.n_steps, st.t_compare,
+          data_.data() + i * n_groups_data_, n_groups_data_);
+      }
       if (timing_) {
         record(ev_step_[2 * i + 1]);
       }
@@ -779,6 +863,10 @@ private:
       k_reorder<<<NT, TS, 0, s>>>(cur, other, L.stride, S.n_state(),
                                   L.tiles.empty() ? nullptr : S.tiles_dev(),
                                   offset_.data(), idx_.data(), mode_.data());
+      if constexpr (is_continuous<T>()) {
+        owner_->enqueue_reorder_record(S.tiles_dev(), NT, TS, offset_.data(),
+                                       idx_.data(), mode_.data(), s);
+      }
       std::swap(cur, other);
       const std::size_t stride = L.stride;
       if (save_traj_ || !snap_obs_.empty()) {
@@ -875,7 +963,15 @@ private:
     graph_state_ptr_ = sys_->state_ptr();
   }
 
-  std::unique_ptr<discrete_system<T>> sys_;
+  static discrete_system<T>& base_of(discrete_system<T>& s) {
+    return s;
+  }
+  static discrete_system<T>& base_of(continuous_system<T>& s) {
+    return s.base();
+  }
+
+  std::unique_ptr<system_type> owner_;
+  discrete_system<T>* sys_;
   double time_start_;
   std::vector<double> times_;
   int n_groups_data_;

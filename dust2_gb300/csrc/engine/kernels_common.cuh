@@ -126,6 +126,23 @@ static __global__ void k_reorder(const double* __restrict__ src,
   }
 }
 
+// k_reorder for one row of integers (solver step counters).
+static __global__ void k_reorder_int(const int* __restrict__ src,
+                                     int* __restrict__ dst, int stride,
+                                     const tile* __restrict__ tiles,
+                                     const int* __restrict__ group_offset,
+                                     const int* __restrict__ index,
+                                     const int* __restrict__ group_mode) {
+  const tile tl = tiles[blockIdx.x];
+  if (static_cast<int>(threadIdx.x) >= tl.count) {
+    return;
+  }
+  const int k = tl.start + threadIdx.x;
+  const bool move = group_mode == nullptr || group_mode[tl.group] != 0;
+  dst[k] = src[move ? group_offset[tl.group] + index[k] : k];
+  (void)stride;
+}
+
 inline int n_blocks(long n, int block) {
   return static_cast<int>((n + block - 1) / block);
 }

@@ -34,6 +34,7 @@ struct system_factory {
                                double time_start, const double* times,
                                int n_times, const double* data,
                                int n_groups_data, double dt,
+                               const ode_control& control,
                                const std::vector<std::uint64_t>& rng_words,
                                int tile_size);
   // nullptr for systems without a filter (continuous time, no compare).
@@ -55,8 +56,10 @@ std::vector<const system_factory*> all_systems();
 template <typename T>
 std::string system_info_json() {
   std::ostringstream s;
+  s.precision(17);
   s << "{\"name\": \"" << T::name << "\", \"time_type\": \""
-    << (is_continuous<T>() ? "continuous" : "discrete") << "\""
+    << (is_mixed_time<T>() ? "mixed" :
+        is_continuous<T>() ? "continuous" : "discrete") << "\""
     << ", \"has_compare\": "
     << (has_compare_data<T>::value ? "true" : "false")
     << ", \"has_adjoint\": "

@@ -116,7 +116,7 @@ DUST2_PARTICLE_KERNEL(T) k_unfilter_discrete(
 template <typename T>
 DUST2_PARTICLE_KERNEL(T) k_unfilter_ode(
     system_view<T> v, ode_view o, dopri5::control_dev ctl, double time0,
-    const double* times, int n_times, const int* requires_init,
+    double dt, const double* times, int n_times, const int* requires_init,
     const int* active, const typename T::data_type* data, int n_groups_data,
     double* ll, unfilter_save sv) {
   constexpr int NV = n_var_max<T>();
@@ -138,7 +138,7 @@ DUST2_PARTICLE_KERNEL(T) k_unfilter_ode(
   if constexpr (has_compare_data<T>::value) {
     const auto& shared = mixed ? v.shared[g] : sm.shared();
     const zero_every_spec& zero = mixed ? v.zero_every[g] : sm.zero;
-    const int n_var = v.n_state - T::n_output;
+    const int n_var = v.n_state - T::n_output - n_special<T>();
     auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
     typename T::internal_state internal{};
     double y[T::n_state_max];
@@ -147,15 +147,18 @@ DUST2_PARTICLE_KERNEL(T) k_unfilter_ode(
     dopri5::scratch<NV> s;
     load_ode<NV>(o, k, n_var, st);
     dopri5::solver<T, NV> sol{ctl, shared, internal, n_var, k};
+    sol.n_special = n_special<T>();
     if (requires_init[g]) {
       sol.initialise(time0, y, st, s);
     }
     double t = time0;
     double acc = 0;
+    int update_err = 0;
     for (int i = 0; i < n_times; ++i) {
       const double t_end = times[i];
-      if (st.err == 0) {
-        sol.run(t, t_end, y, zero, st, s);
+      if (st.err == 0 && update_err == 0) {
+        update_err = advance<T, NV>(sol, t, t_end, dt, y, zero, st, s, rng,
+                                    shared, internal);
       }
       t = t_end;
       const auto& d = data[static_cast<long>(i) * n_groups_data +
@@ -176,8 +179,8 @@ DUST2_PARTICLE_KERNEL(T) k_unfilter_ode(
     store_state<T>(v, k, y);
     store_ode<NV>(o, k, n_var, st);
     ll[k] = acc;
-    if (st.err != 0) {
-      rng.err = st.err;
+    if (st.err != 0 || update_err != 0) {
+      rng.err = st.err != 0 ? st.err : update_err;
     }
     capture_error(v.errors, v.any_error, k, rng);
   }

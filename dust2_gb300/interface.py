@@ -95,6 +95,10 @@ def logistic():
     return Generator("logistic")
 
 
+def malaria():
+    return Generator("malaria")
+
+
 def seir_age():
     return Generator("seir_age")
 
@@ -146,12 +150,16 @@ def _scalar_size(x, name, allow_zero=False):
 
 
 def _check_dt(dt, generator):
+    """R/filter-support.R check_system_dt: none for continuous time; a
+    mixed-time system may go without (no updates, returned as 0)."""
     if generator.time_type == "continuous":
         if dt is not None:
             raise DustError("Can't use 'dt' with continuous-time systems")
         return None
     if dt is None:
         dt = generator.default_dt
+    if dt is None and generator.time_type == "mixed":
+        return 0.0
     dt = float(dt)
     if dt <= 0:
         raise DustError("Expected 'dt' to be greater than 0")
@@ -324,7 +332,7 @@ def dust_system_create(generator, pars=None, n_particles=1, n_groups=1,
     flat = as_f64(np.concatenate([gen.pack_pars(p) for p in pars]))
     ctl = None
     ctl_struct = None
-    if gen.time_type == "continuous":
+    if gen.time_type != "discrete":
         ctl = ode_control if ode_control is not None else dust_ode_control()
         ctl_struct, _keep = _ode_control_struct(ctl)
     words = _seed_words(seed)
@@ -533,7 +541,7 @@ def _check_times(times, dt, name="times"):
         if bad.size > 5:
             msg += f"\n...and {bad.size - 4} other errors"
         raise DustError(msg)
-    if dt is not None and dt <= 1:
+    if dt is not None and 0 < dt <= 1:
         rem = _fmod(times, dt)
         bad = np.nonzero(np.abs(rem) > math.sqrt(np.finfo(float).eps))[0]
         if bad.size:
@@ -730,8 +738,9 @@ class DustLikelihood:
 
     def __init__(self, generator, time_start, data, n_particles, n_groups,
                  dt, initial_rng_state, preserve_group_dimension,
-                 n_particles_per_group=None):
+                 n_particles_per_group=None, ode_control=None):
         self.generator = generator
+        self.ode_control = ode_control
         self.time_start = time_start
         self.data = data
         self.n_particles = n_particles
@@ -757,7 +766,21 @@ class DustLikelihood:
         words = np.frombuffer(self.initial_rng_state,
                               dtype="<u8").astype(np.uint64)
         handle = ctypes.c_void_p()
-        if self.n_particles_per_group is None:
+        if self.generator.time_type == "mixed":
+            if self.n_particles_per_group is not None:
+                raise DustError("Mixed-time filters need equal particle "
+                                "counts per group")
+            c = self.ode_control if self.ode_control is not None else \
+                dust_ode_control()
+            ctl, keep = _ode_control_struct(c)
+            check(_lib.lib().dust2_gb300_filter_alloc_continuous(
+                self.generator.name.encode(), dptr(flat), self.n_groups,
+                self.n_particles, self.time_start, dptr(times), times.size,
+                dptr(rows), self.data["n_groups_data"], self.dt,
+                ctypes.byref(ctl), uptr(words), words.size,
+                ctypes.byref(handle)))
+            del keep
+        elif self.n_particles_per_group is None:
             check(_lib.lib().dust2_gb300_filter_alloc(
                 self.generator.name.encode(), dptr(flat), self.n_groups,
                 self.n_particles, self.time_start, dptr(times), times.size,
@@ -813,6 +836,8 @@ def dust_filter_create(generator, time_start, data, n_particles,
     if gen.time_type == "continuous":
         raise DustError(
             "Can't use 'dust_filter_create()' with continuous-time models")
+    if gen.time_type == "discrete" and ode_control is not None:
+        raise DustError("Can't use 'ode_control' with discrete-time systems")
     dt = _check_dt(dt, gen)
     n_groups = d["n_groups"]
     if uneven and len(npg) != n_groups:
@@ -824,7 +849,7 @@ def dust_filter_create(generator, time_start, data, n_particles,
     return DustLikelihood(gen, time_start, d,
                           max(npg) if uneven else n_particles, n_groups, dt,
                           initial, preserve_group_dimension,
-                          npg if uneven else None)
+                          npg if uneven else None, ode_control)
 
 
 class DustUnfilter:
@@ -858,7 +883,7 @@ class DustUnfilter:
         times = as_f64(self.data["time"])
         ctl = None
         keep = None
-        if self.generator.time_type == "continuous":
+        if self.generator.time_type != "discrete":
             c = self.ode_control if self.ode_control is not None else \
                 dust_ode_control()
             ctl, keep = _ode_control_struct(c)
@@ -908,6 +933,8 @@ def dust_unfilter_create(generator, time_start, data, n_particles=1,
         if ode_control is not None:
             raise DustError(
                 "Can't use 'ode_control' with discrete-time systems")
+        dt = _check_dt(dt, gen)
+    elif gen.time_type == "mixed":
         dt = _check_dt(dt, gen)
     elif dt is not None:
         raise DustError("Can't use 'dt' with continuous-time systems")

@@ -216,6 +216,18 @@ int dust2_gb300_filter_alloc(const char* name, const double* pars,
                              const uint64_t* seed, size_t seed_len,
                              dust2_gb300_filter** out);
 
+/* dust2_continuous_filter_alloc (r/continuous/filter.hpp:13-90) for
+ * mixed-time systems (an ODE with a discrete-time update every dt; dt = 0
+ * runs the ODE alone).  Pure continuous-time systems are refused, as
+ * R/interface-filter.R:59-65 refuses them.  control NULL = the defaults
+ * of dust_ode_control.  Otherwise as dust2_gb300_filter_alloc. */
+int dust2_gb300_filter_alloc_continuous(
+    const char* name, const double* pars, size_t n_groups,
+    size_t n_particles, double time_start, const double* time, size_t n_time,
+    const double* data, size_t n_groups_data, double dt,
+    const dust2_gb300_ode_control* control, const uint64_t* seed,
+    size_t seed_len, dust2_gb300_filter** out);
+
 /* As dust2_gb300_filter_alloc with a particle count per group (groups of
  * uneven size share one launch; dust2 itself requires equal counts). */
 int dust2_gb300_filter_alloc_uneven(const char* name, const double* pars,

@@ -29,6 +29,7 @@
 
 #include "engine/error_text.hpp"
 #include "systems/logistic.hpp"
+#include "systems/malaria.hpp"
 #include "systems/seir_age.hpp"
 #include "systems/sir.hpp"
 #include "systems/sir_cases.hpp"
@@ -505,12 +506,21 @@ struct dopri5_port {
     k3(n_var), k4(n_var), k5(n_var), k6(n_var),
     facc1(1 / c.factor_min), facc2(1 / c.factor_max) {}
 
+  // special state (mixed-time systems) following the n ODE variables:
+  // read by the rhs, constant through a run (solver.hpp:236-239)
+  std::vector<double> special;
+
+  void set_special(const double* y) {
+    std::copy(y + n, y + n + special.size(), special.begin());
+  }
+
   void rhs(double t, const double* y, double* dy) {
     typename S::internal_state internal{};
-    // systems may read state beyond the ODE variables (outputs); pass a
-    // buffer large enough for the full state
+    // systems may read state beyond the ODE variables (specials,
+    // outputs); pass a buffer large enough for the full state
     double buf[S::n_state_max] = {};
     std::copy_n(y, n, buf);
+    std::copy(special.begin(), special.end(), buf + n);
     double out[S::n_state_max] = {};
     S::rhs(t, buf, shared, internal, out);
     std::copy_n(out, n, dy);
@@ -689,6 +699,7 @@ struct dopri5_port {
   // solver.hpp:232-262
   void run(double t, double t_end, double* y, const zero_list& z,
            ode_internals& in) {
+    set_special(y);
     const auto& ct = ctl.critical_times;
     if (ct.empty()) {
       while (t < t_end) {
@@ -712,6 +723,7 @@ struct dopri5_port {
 
   // solver.hpp:265-324
   void initialise(double t, const double* y, ode_internals& in) {
+    set_special(y);
     in.step_size = 0;
     in.error = 0;
     in.n_steps = 0;
@@ -783,6 +795,77 @@ void ode_simulate(const double* pars, int n_groups, int n_particles,
         if constexpr (dust2gpu::has_output<S>::value) {
           S::output(t, y.data(), shared[g], internal);
         }
+        std::copy(y.begin(), y.end(),
+                  out + (static_cast<size_t>(i) * n_total + k) * n_state);
+      }
+    } catch (const std::exception& e) {
+      err.e[k].code = std::string(e.what()) == "too many steps" ?
+        dust2gpu::ERR_ODE_TOO_MANY_STEPS : dust2gpu::ERR_ODE_STEP_TOO_SMALL;
+    }
+    stats[3 * k] = in.n_steps;
+    stats[3 * k + 1] = in.n_steps_accepted;
+    stats[3 * k + 2] = in.n_steps_rejected;
+  }
+  err.report();
+}
+
+// A mixed-time system (continuous/system.hpp:80-106, 544-585) from its
+// initial conditions through `times`.  Between output times: with dt = 0
+// the ODE alone; otherwise n = (t_end - t) / dt truncated steps, step s
+// integrating to t + s dt (the last to t_end; the first is empty), each
+// followed by the update at t_end with a copy of the particle's generator
+// (never advanced) applied to a copy of the state, and a re-initialisation
+// of the solver at t when the state changed.
+template <typename S>
+void mixed_simulate(const double* pars, int n_groups, int n_particles,
+                    double time, double dt, const ode_ctl& ctl,
+                    const uint64_t* rng_words, const double* times,
+                    int n_times, double* out, int64_t* stats) {
+  auto shared = shared_of<S>(pars, n_groups);
+  const int n_state = S::n_state(shared[0]);
+  const int n_special = dust2gpu::n_special<S>();
+  const int n_variables = n_state - S::n_output;
+  const int n_var = n_variables - n_special;
+  const size_t n_total = static_cast<size_t>(n_particles) * n_groups;
+  auto rngs = make_rng(rng_words, n_total, false);
+  errors err(n_total);
+  for (size_t k = 0; k < n_total; ++k) {
+    const int g = k / n_particles;
+    typename S::internal_state internal{};
+    std::vector<double> y(n_state, 0.0), y_other(n_state, 0.0);
+    S::initial(time, shared[g], internal, rngs[k], y.data());
+    ode_internals in(n_var);
+    dopri5_port<S> sol(ctl, shared[g], n_var);
+    sol.special.resize(n_special);
+    const auto z = zero_every_of<S>(shared[g]);
+    try {
+      sol.initialise(time, y.data(), in);
+      double t = time;
+      for (int i = 0; i < n_times; ++i) {
+        const double t_end = times[i];
+        if (dt == 0) {
+          sol.run(t, t_end, y.data(), z, in);
+        } else if (t_end > t) {
+          const long n_steps = static_cast<long>((t_end - t) / dt);
+          double t1 = t;
+          for (long step = 0; step < n_steps; ++step) {
+            const double t0 = t1;
+            t1 = (step == n_steps - 1) ? t_end : t + step * dt;
+            sol.run(t0, t1, y.data(), z, in);
+            std::copy_n(y.begin(), n_variables, y_other.begin());
+            rng_t r = rngs[k];
+            S::update(t_end, dt, y.data(), shared[g], internal, r,
+                      y_other.data());
+            const bool same = std::equal(y_other.begin(),
+                                         y_other.begin() + n_variables,
+                                         y.begin());
+            std::copy_n(y_other.begin(), n_variables, y.begin());
+            if (!same) {
+              sol.initialise(t, y.data(), in);
+            }
+          }
+        }
+        t = t_end;
         std::copy(y.begin(), y.end(),
                   out + (static_cast<size_t>(i) * n_total + k) * n_state);
       }
@@ -1303,6 +1386,36 @@ int oracle_ode_simulate(const char* name, const double* pars, int n_groups,
     } else {
       throw std::runtime_error("unknown system " + nm);
     }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// mixed_simulate for the named mixed-time system; rng: 4 words per
+// particle.
+int oracle_mixed_simulate(const char* name, const double* pars, int n_groups,
+                          int n_particles, double time, double dt,
+                          int max_steps, double atol, double rtol,
+                          double step_size_min, double step_size_max,
+                          const uint64_t* rng, const double* times,
+                          int n_times, double* out, int64_t* stats_out,
+                          char* err, int err_len) {
+  try {
+    ode_ctl ctl;
+    ctl.max_steps = max_steps;
+    ctl.atol = atol;
+    ctl.rtol = rtol;
+    ctl.step_size_min = step_size_min;
+    ctl.step_size_max = step_size_max;
+    const std::string nm(name);
+    if (nm != "malaria") {
+      throw std::runtime_error("unknown system " + nm);
+    }
+    mixed_simulate<dust2gpu::systems::malaria>(
+      pars, n_groups, n_particles, time, dt, ctl, rng, times, n_times, out,
+      stats_out);
     return 0;
   } catch (const std::exception& e) {
     set_err(err, err_len, e.what());

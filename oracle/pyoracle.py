@@ -188,6 +188,58 @@ class Oracle:
         self._call(self._unf, *args)
         return ll.reshape(n_runs, n_groups, n_particles), state
 
+    def mixed_simulate(self, name, pars, n_groups, n_particles, time, dt,
+                       rng, times, n_state, max_steps=10000, atol=1e-6,
+                       rtol=1e-6, step_size_min=np.finfo(float).eps,
+                       step_size_max=np.inf):
+        """A mixed-time system (dust_continuous with updates every dt)
+        from its initial conditions through `times`; rng: 4 words per
+        particle.  Returns (state [time][group][particle][state], solver
+        counts [particle][3])."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        rng = np.ascontiguousarray(rng, dtype=np.uint64)
+        n_total = n_groups * n_particles
+        out = np.empty(times.size * n_total * n_state)
+        stats = np.empty(3 * n_total, dtype=np.int64)
+        self._call(getattr(self.lib, self.prefix + "mixed_simulate"),
+                   _c(name.encode()), _dp(pars), _n(n_groups),
+                   _n(n_particles), ctypes.c_double(time),
+                   ctypes.c_double(dt), _n(max_steps), ctypes.c_double(atol),
+                   ctypes.c_double(rtol), ctypes.c_double(step_size_min),
+                   ctypes.c_double(step_size_max), rng.ctypes.data_as(_u),
+                   _dp(times), _n(times.size), _dp(out),
+                   stats.ctypes.data_as(_l))
+        return (out.reshape(times.size, n_groups, n_particles, n_state),
+                stats.reshape(n_total, 3))
+
+    def mixed_filter_run(self, name, pars, n_groups, n_particles,
+                         time_start, times, data, n_groups_data, dt, rng,
+                         n_state, n_runs=1, max_steps=10000, atol=1e-6,
+                         rtol=1e-6, step_size_min=np.finfo(float).eps,
+                         step_size_max=np.inf):
+        """Particle filter runs over a mixed-time system; returns (ll
+        [n_runs][group], final state [group][particle][state], raw
+        generator state)."""
+        pars = np.ascontiguousarray(pars, dtype=np.float64)
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        rng = np.ascontiguousarray(rng, dtype=np.uint64)
+        ll = np.empty(n_runs * n_groups)
+        state = np.empty(n_groups * n_particles * n_state)
+        rng_out = np.empty(rng.size, dtype=np.uint64)
+        self._call(getattr(self.lib, self.prefix + "mixed_filter_run"),
+                   _c(name.encode()), _dp(pars), _n(n_groups),
+                   _n(n_particles), ctypes.c_double(time_start), _dp(times),
+                   _n(times.size), _dp(data), _n(n_groups_data),
+                   ctypes.c_double(dt), _n(max_steps), ctypes.c_double(atol),
+                   ctypes.c_double(rtol), ctypes.c_double(step_size_min),
+                   ctypes.c_double(step_size_max), rng.ctypes.data_as(_u),
+                   _n(n_runs), _dp(ll), _dp(state),
+                   rng_out.ctypes.data_as(_u))
+        return (ll.reshape(n_runs, n_groups),
+                state.reshape(n_groups, n_particles, n_state), rng_out)
+
     def unfilter_states(self, name, pars, n_groups, n_particles, time_start,
                         times, data, n_groups_data, n_state, dt=1.0,
                         max_steps=10000, atol=1e-6, rtol=1e-6,

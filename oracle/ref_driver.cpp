@@ -28,6 +28,7 @@
 
 #include "engine/error_text.hpp"
 #include "systems/logistic.hpp"
+#include "systems/malaria.hpp"
 #include "systems/seir_age.hpp"
 #include "systems/sir.hpp"
 #include "systems/sir_cases.hpp"
@@ -181,6 +182,33 @@ struct ref_continuous {
   static dust2::zero_every_type<real_type> zero_every(
       const shared_state& shared) {
     return zero_every_of<S>(shared);
+  }
+};
+
+// A mixed-time system (rhs + update) for dust_continuous: the special
+// entries are the last packing block, counted by size_special
+// (properties.hpp:130-153).
+template <typename S>
+struct ref_mixed : ref_continuous<S> {
+  using real_type = double;
+  using rng_state_type = ::rng_state_type;
+  using shared_state = typename S::shared_state;
+  using internal_state = typename S::internal_state;
+
+  static dust2::packing packing_state(const shared_state& shared) {
+    const size_t n = S::n_state(shared);
+    return dust2::packing{
+      {"state", {n - S::n_special}},
+      {"special", {static_cast<size_t>(S::n_special)}}};
+  }
+  static size_t size_special() {
+    return 1;
+  }
+  static void update(real_type time, real_type dt, const real_type* state,
+                     const shared_state& shared, internal_state& internal,
+                     rng_state_type& rng, real_type* state_next) {
+    S::update(time, dt, state, shared, internal, rng, state_next);
+    raise_if_error(rng);
   }
 };
 
@@ -466,6 +494,119 @@ int ref_ode_simulate(const char* name, const double* pars, int n_groups,
   }
 }
 
+// dust_continuous over a mixed-time system (continuous/system.hpp:80-106,
+// 544-585): initial conditions, then run_to_time through `times`
+// recording state.  dt = 0 runs the ODE alone.  rng: 4 words per particle
+// (the particles' streams).  stats_out: [particle][3] n_steps, accepted,
+// rejected.
+int ref_mixed_simulate(const char* name, const double* pars, int n_groups,
+                       int n_particles, double time, double dt,
+                       int max_steps, double atol, double rtol,
+                       double step_size_min, double step_size_max,
+                       const uint64_t* rng, const double* times, int n_times,
+                       double* out, int64_t* stats_out, char* err,
+                       int err_len) {
+  try {
+    const std::string nm(name);
+    if (nm != "malaria") {
+      throw std::runtime_error("unknown system " + nm);
+    }
+    using S = dust2gpu::systems::malaria;
+    using T = ref_mixed<S>;
+    auto shared = shared_of<S>(pars, n_groups);
+    std::vector<typename T::internal_state> internal(n_groups);
+    dust2::ode::control<double> ctl(max_steps, atol, rtol, step_size_min,
+                                    step_size_max, {}, false, false);
+    const size_t n_total = static_cast<size_t>(n_particles) * n_groups;
+    std::vector<uint64_t> seed(rng, rng + 4 * n_total);
+    dust2::dust_continuous<T> sys(shared, internal, time, dt, ctl,
+                                  n_particles, seed, false, 1);
+    sys.set_state_initial(sys.all_groups());
+    const size_t len = sys.state().size();
+    for (int i = 0; i < n_times; ++i) {
+      sys.run_to_time(times[i], sys.all_groups());
+      const auto& st = sys.state();
+      std::copy(st.begin(), st.end(), out + i * len);
+    }
+    const auto& oi = sys.ode_internals();
+    for (size_t k = 0; k < oi.size(); ++k) {
+      stats_out[3 * k] = oi[k].n_steps;
+      stats_out[3 * k + 1] = oi[k].n_steps_accepted;
+      stats_out[3 * k + 2] = oi[k].n_steps_rejected;
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
+// dust2::filter over dust_continuous for a mixed-time system, following
+// dust2_continuous_filter_alloc (r/continuous/filter.hpp:13-86) for the
+// stream split; otherwise as ref_filter_run (n_runs runs of the same
+// object; ll_out [n_runs][n_groups]; state_out; rng_out in the raw layout
+// of r/filter.hpp:273-298).
+int ref_mixed_filter_run(const char* name, const double* pars, int n_groups,
+                         int n_particles, double time_start,
+                         const double* times, int n_times, const double* data,
+                         int n_groups_data, double dt, int max_steps,
+                         double atol, double rtol, double step_size_min,
+                         double step_size_max, const uint64_t* rng,
+                         int n_runs, double* ll_out, double* state_out,
+                         uint64_t* rng_out, char* err, int err_len) {
+  try {
+    const std::string nm(name);
+    if (nm != "malaria") {
+      throw std::runtime_error("unknown system " + nm);
+    }
+    using S = dust2gpu::systems::malaria;
+    using T = ref_mixed<S>;
+    auto shared = shared_of<S>(pars, n_groups);
+    std::vector<typename T::internal_state> internal(n_groups);
+    dust2::ode::control<double> ctl(max_steps, atol, rtol, step_size_min,
+                                    step_size_max, {}, false, false);
+    std::vector<uint64_t> seed_filter, seed_system;
+    for (int g = 0; g < n_groups; ++g) {
+      const uint64_t* it = rng + static_cast<size_t>(g) * 4 *
+        (n_particles + 2);
+      seed_filter.insert(seed_filter.end(), it, it + 8);
+      seed_system.insert(seed_system.end(), it + 8,
+                         it + 4 * (n_particles + 2));
+    }
+    dust2::dust_continuous<T> sys(shared, internal, time_start, dt, ctl,
+                                  n_particles, seed_system, false, 1);
+    std::vector<double> tt(times, times + n_times);
+    std::vector<typename S::data_type> d;
+    const int nd = sizeof(typename S::data_type) / sizeof(double);
+    for (int i = 0; i < n_times * n_groups_data; ++i) {
+      d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+    }
+    dust2::filter<dust2::dust_continuous<T>> obj(sys, time_start, tt, d,
+                                                 seed_filter);
+    for (int r = 0; r < n_runs; ++r) {
+      obj.run(true, false, {}, {}, obj.sys.all_groups());
+      const auto& ll = obj.last_log_likelihood();
+      std::copy(ll.begin(), ll.end(), ll_out + r * n_groups);
+    }
+    std::copy(obj.sys.state().begin(), obj.sys.state().end(), state_out);
+    const auto sf = obj.rng_state();
+    const auto ss = obj.sys.rng_state();
+    size_t pos = 0;
+    for (int g = 0; g < n_groups; ++g) {
+      for (int w = 0; w < 8; ++w) {
+        rng_out[pos++] = sf[g * 8 + w];
+      }
+      for (int w = 0; w < 4 * n_particles; ++w) {
+        rng_out[pos++] = ss[static_cast<size_t>(g) * 4 * n_particles + w];
+      }
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, err_len, e.what());
+    return 1;
+  }
+}
+
 // dust2::filter::run with save_trajectories and snapshots
 // (filter.hpp:42-104) and the export of both with reordering
 // (trajectories.hpp:135-268, as r/filter.hpp:55-137 calls it);
@@ -585,6 +726,21 @@ int ref_unfilter_run(const char* name, const double* pars, int n_groups,
       dust2::ode::control<double> ctl(max_steps, atol, rtol, step_size_min,
                                       step_size_max, {}, false, false);
       dust2::dust_continuous<T> sys(shared, internal, time_start, 0, ctl,
+                                    n_particles, seed, true, 1);
+      dust2::unfilter<dust2::dust_continuous<T>> obj(sys, time_start, tt,
+                                                     data_of(tag<S>{}));
+      finish(obj);
+      return 0;
+    }
+    if (nm == "malaria") {
+      // mixed time: dt is the update interval (0: none)
+      using S = dust2gpu::systems::malaria;
+      using T = ref_mixed<S>;
+      auto shared = shared_of<S>(pars, n_groups);
+      std::vector<typename T::internal_state> internal(n_groups);
+      dust2::ode::control<double> ctl(max_steps, atol, rtol, step_size_min,
+                                      step_size_max, {}, false, false);
+      dust2::dust_continuous<T> sys(shared, internal, time_start, dt, ctl,
                                     n_particles, seed, true, 1);
       dust2::unfilter<dust2::dust_continuous<T>> obj(sys, time_start, tt,
                                                      data_of(tag<S>{}));

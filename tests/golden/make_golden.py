@@ -10,7 +10,7 @@ on the engine under test.
 
 Run from the repository root:  python tests/golden/make_golden.py
 (`--unfilter` / `--trajectories` / `--adjoint` /
-`--unfilter-trajectories` write only those fixtures).
+`--unfilter-trajectories` / `--mixed` write only those fixtures).
 """
 
 import sys
@@ -145,6 +145,7 @@ def main():
     trajectories(ref)
     adjoints(ref)
     unfilter_trajectories(ref)
+    mixed(ref)
 
 
 def unfilters(ref):
@@ -264,8 +265,65 @@ def unfilter_trajectories(ref):
          full_ode=full_o, snap_ode=snap_o)
 
 
+MIXED_SIMULATE_CASES = [
+    # (label, dt, output times)
+    ("ode_only", 0.0, [float(t) for t in range(21)]),
+    ("daily", 1.0, [float(t) for t in range(21)]),
+    ("coarse", 1.0, [4.0, 8.0, 12.0, 16.0]),
+    ("uneven", 2.0, [3.0, 5.0, 9.0, 10.0, 16.0]),
+]
+
+
+def mixed(ref):
+    """12. Mixed-time systems (continuous/system.hpp:80-106, 544-585,
+    test-malaria.R, test-filter.R "can run filter on mixed time models"):
+    the malaria system, 2 groups (a = 1/3 and 0.4) x 4 particles from
+    seeded streams, through each case of MIXED_SIMULATE_CASES; filters of
+    1 group x 100 particles (the reference test's data, dt = 1, 5 runs)
+    and 3 groups x 40 particles (per-group data, dt = 0.5, 3 runs); an
+    unfilter of 2 groups at dt = 1."""
+    pars = workload_data.pack("malaria", [{}, {"a": 0.4}])
+    rng = xoshiro.streams(13, 8)
+    out = {"sim_pars": pars, "sim_rng": rng}
+    for label, dt, times in MIXED_SIMULATE_CASES:
+        y, stats = ref.mixed_simulate("malaria", pars, 2, 4, 0.0, dt, rng,
+                                      np.array(times), 20)
+        out[f"sim_{label}"] = y
+        out[f"sim_{label}_stats"] = stats
+    times = np.array([4.0, 8, 12, 16])
+    data = np.array([[2.0, 1], [4, 2], [6, 3], [8, 3]])
+    p1 = workload_data.pack("malaria", [{}])
+    rng1 = xoshiro.streams(42, 102)
+    ll, state, rng_out = ref.mixed_filter_run(
+        "malaria", p1, 1, 100, 0.0, times, data.ravel(), 1, 1.0, rng1, 20,
+        n_runs=5)
+    out.update(f1_pars=p1, f1_times=times, f1_data=data, f1_rng=rng1,
+               f1_ll=ll, f1_state=state, f1_rng_out=rng_out)
+    p3 = workload_data.pack("malaria", [{"a": 0.3}, {"a": 0.35},
+                                        {"r": 0.02}])
+    rs = np.random.default_rng(12)
+    times3 = np.arange(2.0, 31.0, 2.0)
+    tested = rs.integers(5, 30, (times3.size, 3)).astype(float)
+    positive = np.floor(tested * rs.uniform(0.6, 0.95, tested.shape))
+    data3 = np.stack([tested, positive], axis=-1)
+    rng3 = xoshiro.streams(5, 3 * 42)
+    ll3, state3, rng3_out = ref.mixed_filter_run(
+        "malaria", p3, 3, 40, 0.0, times3, data3.ravel(), 3, 0.5, rng3, 20,
+        n_runs=3)
+    out.update(f3_pars=p3, f3_times=times3, f3_data=data3, f3_rng=rng3,
+               f3_ll=ll3, f3_state=state3, f3_rng_out=rng3_out)
+    ll_u, state_u = ref.unfilter_run("malaria", pars, 2, 1, 0.0, times,
+                                     np.repeat(data[:, None, :], 2,
+                                               axis=1).ravel(), 2, 20,
+                                     dt=1.0, n_runs=1)
+    out.update(u_times=times, u_data=data, u_ll=ll_u, u_state=state_u)
+    save("mixed_malaria", **out)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["--adjoint"]:
+    if sys.argv[1:] == ["--mixed"]:
+        mixed(pyoracle.ref())
+    elif sys.argv[1:] == ["--adjoint"]:
         adjoints(pyoracle.ref())
     elif sys.argv[1:] == ["--unfilter-trajectories"]:
         unfilter_trajectories(pyoracle.ref())

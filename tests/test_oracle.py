@@ -308,6 +308,30 @@ def test_port_unfilter_states_equal_reference_trajectories(port):
     np.testing.assert_array_equal(states[snap_at], t["snap_ode"])
 
 
+@pytest.mark.parametrize("label,dt", [("ode_only", 0.0), ("daily", 1.0),
+                                      ("coarse", 1.0), ("uneven", 2.0)])
+def test_port_mixed_simulate_equals_reference_engine(port, label, dt):
+    """Mixed time (continuous/system.hpp:544-585): the restatement against
+    dust2's own dust_continuous, exactly (same arithmetic, same pow)."""
+    g = golden("mixed_malaria")
+    times = {"ode_only": np.arange(21.0), "daily": np.arange(21.0),
+             "coarse": np.array([4.0, 8, 12, 16]),
+             "uneven": np.array([3.0, 5, 9, 10, 16])}[label]
+    y, stats = port.mixed_simulate("malaria", g["sim_pars"], 2, 4, 0.0, dt,
+                                   g["sim_rng"], times, 20)
+    np.testing.assert_array_equal(y, g[f"sim_{label}"])
+    np.testing.assert_array_equal(stats, g[f"sim_{label}_stats"])
+
+
+def test_reference_mixed_filter_reproduces_fixture(ref):
+    g = golden("mixed_malaria")
+    ll, state, rng_out = ref.mixed_filter_run(
+        "malaria", g["f1_pars"], 1, 100, 0.0, g["f1_times"],
+        g["f1_data"].ravel(), 1, 1.0, g["f1_rng"], 20, n_runs=5)
+    np.testing.assert_array_equal(ll, g["f1_ll"])
+    np.testing.assert_array_equal(rng_out, g["f1_rng_out"])
+
+
 def test_port_trajectories_equal_reference_engine(port):
     g = golden("trajectories_sir")
     args = ("sir", g["pars"], 2, int(g["n_particles"]), 0.0, g["times"],
