@@ -48,12 +48,12 @@ sys.path.insert(0, str(ROOT))
 # particle-step of the step+compare kernel, per workload, from the ncu SASS
 # counters of that kernel over a whole likelihood run (summaries under
 # profiles/).  A workload without an entry reports no achieved rate.
-FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 274.7, "seir_batched": 4552.2,
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 259.6, "seir_batched": 4552.2,
                               "ode_batched": 761.7}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
-FP64_PIPE_INST_PER_UNIT = {"sir_batched": 219.5, "seir_batched": 3542.1,
+FP64_PIPE_INST_PER_UNIT = {"sir_batched": 209.4, "seir_batched": 3542.1,
                            "ode_batched": 641.3}
 
 

@@ -22,7 +22,18 @@ struct sir_cases {
     real_type beta;
     real_type gamma;
   };
-  struct internal_state {};
+  // Per-thread scratch (dust2's internal_state): the recovery
+  // probability 1 - exp(-gamma dt) and the terms of its binomial draws
+  // that depend on p alone (random::binomial_prepare) are the same at
+  // every step while gamma and dt are, so they are kept here and
+  // recomputed only when either changes.  The draws are exactly those of
+  // binomial(rng, I, p_IR).
+  struct internal_state {
+    std::uint64_t key_gamma;
+    std::uint64_t key_dt;
+    bool ready;
+    random::binomial_prob b_IR;
+  };
   struct data_type {
     real_type incidence;
   };
@@ -91,9 +102,18 @@ struct sir_cases {
     const auto R = state[2];
     const auto cases_inc = state[3];
     const auto p_SI = 1 - math::exp(-shared.beta * I / shared.N * dt);
-    const auto p_IR = 1 - math::exp(-shared.gamma * dt);
+    const auto key_gamma = math::bits_of(shared.gamma);
+    const auto key_dt = math::bits_of(dt);
+    if (!internal.ready || internal.key_gamma != key_gamma ||
+        internal.key_dt != key_dt) {
+      internal.b_IR =
+        random::binomial_prepare(1 - math::exp(-shared.gamma * dt));
+      internal.key_gamma = key_gamma;
+      internal.key_dt = key_dt;
+      internal.ready = true;
+    }
     const auto n_SI = random::binomial(rng_state, S, p_SI);
-    const auto n_IR = random::binomial(rng_state, I, p_IR);
+    const auto n_IR = random::binomial(rng_state, I, internal.b_IR);
     state_next[0] = S - n_SI;
     state_next[1] = I + n_SI - n_IR;
     state_next[2] = R + n_IR;
