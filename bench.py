@@ -57,6 +57,18 @@ FP64_PIPE_INST_PER_UNIT = {"sir_batched": 209.4, "seir_batched": 3542.1,
                            "ode_batched": 641.3}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
+# same kernel, from the same captures; `traffic` is this times the units
+# of one launch.
+DRAM_BYTES_PER_UNIT = {"sir_batched": 19.2, "seir_batched": 1271.7,
+                       "ode_batched": 40.0}
+
+
+def traffic_per_launch(workload, units_per_launch):
+    b = DRAM_BYTES_PER_UNIT.get(workload)
+    return None if b is None else b * units_per_launch
+
+
 def pipe_roofline(workload, units_per_s, peak_tflops):
     """Useful FP64-pipe thread instructions per second against the pipe's
     peak (peak DFMA flops / 2)."""
@@ -389,7 +401,12 @@ def gpu_arm(args, rank, world, local):
         roofline = {
             "bound": "fp64", "kernel": f"k_step_compare<{w['system']}>",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": frac, "traffic": None,
+            "frac": frac,
+            "traffic": traffic_per_launch(args.workload, ps_per_launch),
+            "traffic_source": "ncu dram__bytes_read.sum + "
+                              "dram__bytes_write.sum per particle-step of "
+                              "this kernel over a whole run, times the "
+                              "particle-steps of one launch",
             "peak_source": "measured in-process: DFMA-chain microbenchmark "
                            "(dust2_gb300_fp64_peak); MEASURED_PEAKS.json has no FP64 entry",
             "step_launch_ms": step_launch_ms,
@@ -736,7 +753,7 @@ def ode_arm(args, rank, world, local):
         "roofline": {"bound": "fp64", "kernel": "k_ode_run<sirode>",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": None if achieved is None else achieved / peak,
-                     "traffic": None,
+                     "traffic": traffic_per_launch("ode_batched", steps),
                      "fp64_pipe": pipe_roofline("ode_batched",
                                                 steps / (ms * 1e-3), peak),
                      "flops_basis": "executed FP64 ops per attempted "
