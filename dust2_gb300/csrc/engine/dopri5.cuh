@@ -259,63 +259,71 @@ struct solver {
     }
   }
 
+  // One pass of step's accept/reject loop (solver.hpp:161-226): the error
+  // checks, truncation at t_end, one trial step and its acceptance.
+  // Returns 1 when the step was accepted (t then holds the new time), 0
+  // when it was rejected (h shrunk, reject set; try again) and -1 on an
+  // error (st.err set, t unchanged).
+  DUST2_HD int attempt(double& t, double t_end, double* y, double& h,
+                       bool& reject, state<NV>& st, scratch<NV>& s) {
+    if (st.n_steps > ctl.max_steps) {
+      st.err = ERR_ODE_TOO_MANY_STEPS;
+      return -1;
+    }
+    if (h < ctl.step_size_min) {
+      st.err = ERR_ODE_STEP_TOO_SMALL;
+      return -1;
+    }
+    if (h <= fabs(t) * 2.220446049250313e-16) {
+      st.err = ERR_ODE_STEP_VANISHED;
+      return -1;
+    }
+    const bool truncated = t + h > t_end;
+    if (truncated) {
+      h = t_end - t;
+    }
+    const double err = try_step(t, h, y, st, s);
+    st.n_steps++;
+    const double fac11 = pow(err, ctl.constant);
+    if (err <= 1) {
+      update_interpolation(t, h, y, st, s);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        if (i < n_var) {
+          st.dydt[i] = s.k2[i];
+          y[i] = s.y_next[i];
+        }
+      }
+      st.n_steps_accepted++;
+      record_step_time(truncated ? t_end : t + h);
+      if (!truncated) {
+        const double fac_old = ref_max(st.error, 1e-4);
+        double fac = fac11 / pow(fac_old, ctl.beta);
+        fac = clamp(fac / ctl.factor_safe, ctl.facc2, ctl.facc1);
+        const double h_new = h / fac;
+        const double h_max = reject ? h : ctl.step_size_max;
+        st.step_size = ref_min(h_new, h_max);
+        st.error = err;
+      }
+      t = truncated ? t_end : t + h;
+      return 1;
+    }
+    reject = true;
+    if (st.n_steps_accepted >= 1) {
+      st.n_steps_rejected++;
+    }
+    h /= ref_min(ctl.facc1, fac11 / ctl.factor_safe);
+    return 0;
+  }
+
   // One accepted step (solver.hpp:153-229); returns the new time.
   DUST2_HD double step(double t, double t_end, double* y, state<NV>& st,
                        scratch<NV>& s) {
-    bool success = false;
     bool reject = false;
-    bool truncated = false;
     double h = st.step_size;
-    while (!success) {
-      if (st.n_steps > ctl.max_steps) {
-        st.err = ERR_ODE_TOO_MANY_STEPS;
-        return t;
-      }
-      if (h < ctl.step_size_min) {
-        st.err = ERR_ODE_STEP_TOO_SMALL;
-        return t;
-      }
-      if (h <= fabs(t) * 2.220446049250313e-16) {
-        st.err = ERR_ODE_STEP_VANISHED;
-        return t;
-      }
-      truncated = t + h > t_end;
-      if (truncated) {
-        h = t_end - t;
-      }
-      const double err = try_step(t, h, y, st, s);
-      st.n_steps++;
-      const double fac11 = pow(err, ctl.constant);
-      if (err <= 1) {
-        success = true;
-        update_interpolation(t, h, y, st, s);
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-          if (i < n_var) {
-            st.dydt[i] = s.k2[i];
-            y[i] = s.y_next[i];
-          }
-        }
-        st.n_steps_accepted++;
-        record_step_time(truncated ? t_end : t + h);
-        if (!truncated) {
-          const double fac_old = ref_max(st.error, 1e-4);
-          double fac = fac11 / pow(fac_old, ctl.beta);
-          fac = clamp(fac / ctl.factor_safe, ctl.facc2, ctl.facc1);
-          const double h_new = h / fac;
-          const double h_max = reject ? h : ctl.step_size_max;
-          st.step_size = ref_min(h_new, h_max);
-          st.error = err;
-        }
-      } else {
-        reject = true;
-        if (st.n_steps_accepted >= 1) {
-          st.n_steps_rejected++;
-        }
-        h /= ref_min(ctl.facc1, fac11 / ctl.factor_safe);
-      }
+    while (attempt(t, t_end, y, h, reject, st, s) == 0) {
     }
-    return truncated ? t_end : t + h;
+    return t;
   }
 
   // Dense output of the last step for the zero_every entries of `mask`,
