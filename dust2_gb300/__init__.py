@@ -16,7 +16,8 @@ from .interface import (
     dust_system_set_rng_state, dust_system_set_state,
     dust_system_set_state_initial, dust_system_set_time,
     dust_system_simulate, dust_system_state, dust_system_time,
-    dust_system_update_pars, dust_unfilter_create, logistic, malaria,
+    dust_system_update_pars, dust_unfilter_create, dust_unpack_index,
+    dust_unpack_state, logistic, malaria,
     resample_weight, rng_streams,
     scale_log_weights, seir_age, sir, sir_cases, sirode, walk)
 
@@ -37,6 +38,7 @@ __all__ = [
     "dust_system_set_state", "dust_system_set_state_initial",
     "dust_system_set_time", "dust_system_simulate", "dust_system_state",
     "dust_system_time", "dust_system_update_pars", "dust_unfilter_create",
+    "dust_unpack_index", "dust_unpack_state",
     "logistic", "malaria",
     "resample_weight", "rng_streams", "scale_log_weights", "seir_age", "sir",
     "sir_cases", "sirode", "walk"]

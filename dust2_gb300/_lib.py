@@ -181,6 +181,12 @@ _SIGNATURES = {
         ctypes.c_void_p, c_size_p, c_size_p, c_size_p, c_size_p]),
     "dust2_gb300_unfilter_last_snapshots": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p]),
+    "dust2_gb300_system_packing_state": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, c_size_p]),
+    "dust2_gb300_filter_packing_state": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, c_size_p]),
+    "dust2_gb300_unfilter_packing_state": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t, c_size_p]),
     "dust2_gb300_unfilter_update_pars": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p, c_size_p, ctypes.c_size_t]),
     "dust2_gb300_unfilter_state": (ctypes.c_int, [ctypes.c_void_p,

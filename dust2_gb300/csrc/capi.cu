@@ -320,6 +320,52 @@ int dust2_gb300_system_dim(const dust2_gb300_system* sys, size_t* n_state,
   });
 }
 
+// The state packing as JSON, [{"name": ..., "dims": [...]}, ...], into
+// buf (NUL-terminated, truncated to len); *needed gets the full length.
+static void write_packing(const dust2gpu::engine::system_api& s, char* buf,
+                          size_t len, size_t* needed) {
+  std::string out = "[";
+  bool first = true;
+  for (const auto& e : s.packing_state()) {
+    out += first ? "" : ", ";
+    first = false;
+    out += "{\"name\": \"" + e.name + "\", \"dims\": [";
+    for (std::size_t i = 0; i < e.dims.size(); ++i) {
+      out += (i ? ", " : "") + std::to_string(e.dims[i]);
+    }
+    out += "]}";
+  }
+  out += "]";
+  if (needed != nullptr) {
+    *needed = out.size();
+  }
+  if (buf != nullptr && len > 0) {
+    const std::size_t n = std::min(len - 1, out.size());
+    std::memcpy(buf, out.data(), n);
+    buf[n] = '\0';
+  }
+}
+
+int dust2_gb300_system_packing_state(dust2_gb300_system* sys, char* buf,
+                                     size_t len, size_t* needed) {
+  return guard([&] { write_packing(sysref(sys), buf, len, needed); });
+}
+
+int dust2_gb300_filter_packing_state(dust2_gb300_filter* filter, char* buf,
+                                     size_t len, size_t* needed) {
+  return guard([&] {
+    write_packing(filref(filter).sys(), buf, len, needed);
+  });
+}
+
+int dust2_gb300_unfilter_packing_state(dust2_gb300_unfilter* unfilter,
+                                       char* buf, size_t len,
+                                       size_t* needed) {
+  return guard([&] {
+    write_packing(unfref(unfilter).sys(), buf, len, needed);
+  });
+}
+
 int dust2_gb300_system_state(dust2_gb300_system* sys, double* out) {
   return guard([&] {
     auto& s = sysref(sys);

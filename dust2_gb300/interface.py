@@ -1050,6 +1050,66 @@ def dust_likelihood_run(obj, pars, initial=None, save_trajectories=False,
     return ll
 
 
+def _packing(obj):
+    """[(name, dims)] of the object's state packing (the system class's
+    packing_state)."""
+    if isinstance(obj, DustSystem):
+        fn, ptr = _lib.lib().dust2_gb300_system_packing_state, obj.ptr
+    elif isinstance(obj, (DustLikelihood, DustUnfilter)):
+        if obj.ptr is None:
+            raise DustError("Packer is not yet ready: likelihood has not "
+                            "yet been run")
+        fn = (_lib.lib().dust2_gb300_unfilter_packing_state
+              if isinstance(obj, DustUnfilter) else
+              _lib.lib().dust2_gb300_filter_packing_state)
+        ptr = obj.ptr
+    else:
+        raise DustError("Expected 'obj' to be a 'dust_system' or a "
+                        "'dust_likelihood'")
+    need = ctypes.c_size_t()
+    check(fn(ptr, None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(need.value + 1)
+    check(fn(ptr, buf, len(buf), None))
+    return [(e["name"], list(e["dims"])) for e in json.loads(buf.value)]
+
+
+def dust_unpack_index(obj):
+    """R/tools.R dust_unpack_index (monty_packer's index()): each named
+    block of state and its 1-based positions in the state dimension."""
+    out = {}
+    pos = 0
+    for name, dims in _packing(obj):
+        n = int(np.prod(dims)) if dims else 1
+        out[name] = np.arange(pos + 1, pos + n + 1)
+        pos += n
+    return out
+
+
+def dust_unpack_state(obj, state):
+    """R/tools.R dust_unpack_state (monty_packer's unpack()): split the
+    first (state) dimension of `state` into the named blocks; a scalar
+    block drops that dimension, an array block keeps its own
+    dimensions (column-major, as R arrays)."""
+    state = np.asarray(state)
+    out = {}
+    pos = 0
+    rest = state.shape[1:]
+    for name, dims in _packing(obj):
+        n = int(np.prod(dims)) if dims else 1
+        block = state[pos:pos + n]
+        if not dims:
+            out[name] = block[0]
+        elif len(dims) > 1:
+            out[name] = block.reshape(tuple(dims) + rest, order="F")
+        else:
+            out[name] = block
+        pos += n
+    if pos != state.shape[0]:
+        raise DustError(f"Expected 'state' to have {pos} rows, but it had "
+                        f"{state.shape[0]}")
+    return out
+
+
 def dust_likelihood_last_gradient(obj):
     """R/interface-likelihood.R:309-331, r/unfilter.hpp:153-180: the
     gradient of the last adjoint run's log-likelihood with respect to the

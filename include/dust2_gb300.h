@@ -492,6 +492,20 @@ int dust2_gb300_unfilter_snapshot_dim(dust2_gb300_unfilter* unfilter,
 int dust2_gb300_unfilter_last_snapshots(dust2_gb300_unfilter* unfilter,
                                         double* out);
 
+/* The state packing (packing_state of the system class; the
+ * `packing_state` element that dust2_discrete_alloc,
+ * dust2_discrete_filter_alloc and the unfilter allocators return,
+ * r/discrete/system.hpp:46-53) as JSON, [{"name": "S", "dims": []}, ...],
+ * into buf (NUL-terminated, truncated to len; *needed = full length, may
+ * be NULL).  Used by dust_unpack_state / dust_unpack_index. */
+int dust2_gb300_system_packing_state(dust2_gb300_system* sys, char* buf,
+                                     size_t len, size_t* needed);
+int dust2_gb300_filter_packing_state(dust2_gb300_filter* filter, char* buf,
+                                     size_t len, size_t* needed);
+int dust2_gb300_unfilter_packing_state(dust2_gb300_unfilter* unfilter,
+                                       char* buf, size_t len,
+                                       size_t* needed);
+
 /* dust2_unfilter_<sys>_update_pars (r/unfilter.hpp:10-18). */
 int dust2_gb300_unfilter_update_pars(dust2_gb300_unfilter* unfilter,
                                      const double* pars,

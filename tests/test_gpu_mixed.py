@@ -67,7 +67,12 @@ def test_mixed_without_dt_is_the_ode(built):
     y = d.dust_system_simulate(sys, np.arange(21.0))
     assert y.shape == (20, 10, 21)
     np.testing.assert_array_equal(y, y[:, [0] * 10, :])
-    np.testing.assert_allclose(y[-1], np.log(10 / 9), rtol=1e-15)
+    yy = d.dust_unpack_state(sys, y)
+    assert list(yy) == ["Sh", "Ih", "Sv", "Iv", "Ev", "beta"]
+    assert yy["Ev"].shape == (15, 10, 21) and yy["beta"].shape == (10, 21)
+    np.testing.assert_allclose(yy["beta"], np.log(10 / 9), rtol=1e-15)
+    idx = d.dust_unpack_index(sys)
+    assert list(idx["Ev"]) == list(range(5, 20)) and list(idx["beta"]) == [20]
 
 
 def test_mixed_updates_between_runs_match_ode_segments(built):
