@@ -48,19 +48,19 @@ sys.path.insert(0, str(ROOT))
 # particle-step of the step+compare kernel, per workload, from the ncu SASS
 # counters of that kernel over a whole likelihood run (summaries under
 # profiles/).  A workload without an entry reports no achieved rate.
-FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 259.6, "seir_batched": 4552.2,
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 187.3, "seir_batched": 3203.1,
                               "ode_batched": 761.7}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
-FP64_PIPE_INST_PER_UNIT = {"sir_batched": 209.4, "seir_batched": 3542.1,
+FP64_PIPE_INST_PER_UNIT = {"sir_batched": 162.7, "seir_batched": 2682.7,
                            "ode_batched": 641.3}
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
 # same kernel, from the same captures; `traffic` is this times the units
 # of one launch.
-DRAM_BYTES_PER_UNIT = {"sir_batched": 19.2, "seir_batched": 1271.7,
+DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 1175.8,
                        "ode_batched": 40.0}
 
 

@@ -94,7 +94,63 @@ def main():
     out.append(f"#define DUST2_LN2_128_LO {fmt(lo35)}")
     out.append(f"#define DUST2_INV_LN2_128 {fmt(rn(128 / LN2))}")
     del hi_bits, lo
+    fixed_point_tables(out)
     Path(__file__).with_name("tables.hpp").write_text("\n".join(out) + "\n")
+
+
+def fixed_point_tables(out):
+    """Tables and constants of the integer-arithmetic exp and log: values
+    rounded to the nearest integer after scaling by the stated power of
+    two (90-digit decimal arithmetic)."""
+    getcontext().prec = 90
+    ln2 = Decimal(2).ln()
+
+    def rint(v):
+        return int(Decimal(v).to_integral_value())
+
+    def u64(v):
+        assert 0 <= v < 1 << 64, v
+        return f"0x{v:016x}ull"
+
+    def words(v):
+        """A signed 128-bit integer as (high int64 word, low uint64 word)."""
+        assert -(1 << 127) <= v < 1 << 127, v
+        return v >> 64, v & ((1 << 64) - 1)
+
+    def table(name, vals, per_line=3):
+        out.append(f"#define {name} \\")
+        out.append(",\\\n".join("  " + ", ".join(vals[i:i + per_line])
+                                for i in range(0, len(vals), per_line)))
+
+    out.append("")
+    out.append("// Integer-arithmetic exp and log (math.hpp exp / log):")
+    out.append("// 2^(j/128) * 2^63, j = 0..127")
+    table("DUST2_EXP2_Q63",
+          [u64(rint((ln2 * j / 128).exp() * (Decimal(2) ** 63)))
+           for j in range(128)])
+    j0, j1 = 181, 363
+    out.append("// 256/j * 2^62, j = LOG_J0 + i")
+    table("DUST2_LOG_INV_Q62",
+          [u64(rint(Decimal(256) / j * (Decimal(2) ** 62)))
+           for j in range(j0, j1 + 1)])
+    his, los = [], []
+    for j in range(j0, j1 + 1):
+        h, lo = words(rint((Decimal(j) / 256).ln() * (Decimal(2) ** 96)))
+        his.append(f"{h}ll")
+        los.append(u64(lo))
+    out.append("// log(j/256) * 2^96 = LOG_F96_HI[i] * 2^64 + LOG_F96_LO[i]")
+    table("DUST2_LOG_F96_HI", his)
+    table("DUST2_LOG_F96_LO", los)
+    c = rint(128 / ln2 * (Decimal(2) ** 120))
+    out.append("// 128/ln2 * 2^120 = EXP_C120_HI * 2^64 + EXP_C120_LO")
+    out.append(f"#define DUST2_EXP_C120_HI {u64(c >> 64)}")
+    out.append(f"#define DUST2_EXP_C120_LO {u64(c & ((1 << 64) - 1))}")
+    out.append("// ln2 * 2^64; ln2 * 2^96 = LN2_96_HI * 2^64 + LN2_96_LO")
+    out.append(f"#define DUST2_LN2_Q64 {u64(rint(ln2 * (Decimal(2) ** 64)))}")
+    l96 = rint(ln2 * (Decimal(2) ** 96))
+    out.append(f"#define DUST2_LN2_96_HI {u64(l96 >> 64)}")
+    out.append(f"#define DUST2_LN2_96_LO {u64(l96 & ((1 << 64) - 1))}")
+    getcontext().prec = 60
 
 
 if __name__ == "__main__":

@@ -10,14 +10,17 @@
 // bits.  GB300 executes FP64 at 1/64 of its FP32 rate, so the methods are
 // chosen to need few FP64 operations and no FP64 division:
 //
-//   exp    table-driven (Tang 1989): x = (128 k + j) ln2/128 + r with a
-//          two-part ln2/128 (exact k * hi), |r| <= ln2/256, then
-//          2^(j/128) (double-double table) * (1 + expm1(r)), expm1 by its
-//          Taylor polynomial through r^5, scaled by 2^k.
+//   exp    table-driven (Tang 1989): x = (128 k + j) ln2/128 + r,
+//          |r| <= ln2/256, exp(x) = 2^k 2^(j/128) (1 + expm1(r)), expm1 by
+//          its Taylor polynomial through r^6.  Evaluated in integer fixed
+//          point (exp_fixed, below) for |x| < 704; near overflow and
+//          underflow in FP64 (exp_slow, Taylor through r^5, a double-double
+//          table and a two-part ln2/128).
 //   log    table-driven (Tang 1990): x = 2^e m, m in [sqrt(2)/2, sqrt(2)),
-//          F = j/256 nearest to m, r = (m - F) * (1/F) (m - F exact), then
-//          log(x) = e ln2 + log(F) (double-double table) + log1p(r) by its
-//          Taylor polynomial through r^7.
+//          F = j/256 nearest to m, r = (m - F)/F, then
+//          log(x) = e ln2 + log(F) + log1p(r), log1p by its Taylor
+//          polynomial through r^7; evaluated in integer fixed point
+//          (log_fixed, below).
 //   rcp    1/y from the correctly rounded FP32 reciprocal of (float)y
 //          (cheap on this GPU) refined by two Newton steps in FP64 FMA.
 //   lgamma for x > 0: exact table of log(k!) for integer arguments below
@@ -135,10 +138,21 @@ constexpr double EXP_UNDERFLOW = -0x1.74910d52d3051p+9;
 
 DUST2_TABLE(exp2_hi, 128, DUST2_EXP2_HI)
 DUST2_TABLE(exp2_lo, 128, DUST2_EXP2_LO)
-DUST2_TABLE(log_inv, DUST2_LOG_N, DUST2_LOG_INV)
-DUST2_TABLE(log_hi, DUST2_LOG_N, DUST2_LOG_HI)
-DUST2_TABLE(log_lo, DUST2_LOG_N, DUST2_LOG_LO)
 DUST2_TABLE(recip_int, 129, DUST2_RECIP_INT)
+
+#if defined(__CUDACC__)
+#define DUST2_TABLE_U64(name, n, values)                                  \
+  __device__ const std::uint64_t name##_dev[n] = {values};               \
+  inline const std::uint64_t name##_host[n] = {values};
+#define DUST2_TABLE_I64(name, n, values)                                  \
+  __device__ const std::int64_t name##_dev[n] = {values};                \
+  inline const std::int64_t name##_host[n] = {values};
+#else
+#define DUST2_TABLE_U64(name, n, values)                                  \
+  inline const std::uint64_t name##_host[n] = {values};
+#define DUST2_TABLE_I64(name, n, values)                                  \
+  inline const std::int64_t name##_host[n] = {values};
+#endif
 
 // Integer-pipe helpers.  On this GPU every FP64 instruction (arithmetic,
 // comparison, rounding, conversion) shares one slow pipe, so decisions
@@ -210,30 +224,199 @@ DUST2_HD double exp_slow(double x) {
   return scale2(t_hi + std::fma(t_hi, pm1, t_lo), e);
 }
 
+// ---- integer-arithmetic exp and log --------------------------------------
+//
+// The same methods in fixed point: every operation is an integer
+// instruction, so the evaluation runs on the integer pipes, which this GPU
+// has in far greater width than its FP64 pipe (one FP64 warp instruction
+// holds an SM partition's FP64 unit for 64 cycles; a 64 x 64 -> 128-bit
+// product costs about a third of that on the integer pipe, and overlaps
+// with FP64 work).  Host and device run the same integer arithmetic, so
+// results are identical.  Relative error before the final rounding is
+// below 2^-60: the result is the correctly rounded value except within
+// ~2^-8 ulp of a rounding midpoint, where it may be the other neighbour.
+
+using u128 = unsigned __int128;
+using i128 = __int128;
+
+// The fixed-point cores are compiled once per kernel and called: inlined at
+// every site they would raise the register pressure of the large sampler
+// kernels.
+#if defined(__CUDACC__)
+#define DUST2_MATH_CORE inline __host__ __device__ __noinline__
+#else
+#define DUST2_MATH_CORE inline
+#endif
+
+DUST2_TABLE_U64(exp2_q63, 128, DUST2_EXP2_Q63)
+DUST2_TABLE_U64(log_inv_q62, DUST2_LOG_N, DUST2_LOG_INV_Q62)
+DUST2_TABLE_I64(log_f96_hi, DUST2_LOG_N, DUST2_LOG_F96_HI)
+DUST2_TABLE_U64(log_f96_lo, DUST2_LOG_N, DUST2_LOG_F96_LO)
+
+// (a * b) >> s for signed a, b (arithmetic shift; floor).
+DUST2_HD std::int64_t mul_shift(std::int64_t a, std::int64_t b, int s) {
+  return static_cast<std::int64_t>((static_cast<i128>(a) *
+                                    static_cast<i128>(b)) >> s);
+}
+
+#if defined(__CUDA_ARCH__)
+DUST2_HD int clz64(std::uint64_t v) {
+  return __clzll(static_cast<long long>(v));
+}
+#else
+DUST2_HD int clz64(std::uint64_t v) {
+  return v == 0 ? 64 : __builtin_clzll(v);
+}
+#endif
+
+// v * 2^-scale for a non-zero unsigned 128-bit v, rounded to 53 bits
+// (ties away from zero) with the given sign; the result must be normal.
+DUST2_HD double u128_to_double(u128 v, int scale, bool negative) {
+  const std::uint64_t hi = static_cast<std::uint64_t>(v >> 64);
+  const int p = hi != 0 ? 127 - clz64(hi) :
+    63 - clz64(static_cast<std::uint64_t>(v));  // position of the top bit
+  std::uint64_t m;
+  int top = p;
+  if (p >= 53) {
+    const int sh = p - 52;
+    m = static_cast<std::uint64_t>((v + (static_cast<u128>(1) << (sh - 1)))
+                                   >> sh);
+    if (m >> 53) {
+      m >>= 1;
+      top += 1;
+    }
+  } else {
+    m = static_cast<std::uint64_t>(v) << (52 - p);
+  }
+  const std::uint64_t e = static_cast<std::uint64_t>(top - scale + 1023);
+  return from_bits((negative ? 0x8000000000000000ull : 0ull) | (e << 52) |
+                   (m & 0x000fffffffffffffull));
+}
+
+// exp(x) for 2^-54 <= |x| < 704 (the caller handles the rest).
+//   t = |x| 128/ln2 in fixed point with 64 fraction bits, from the 53-bit
+//       significand times a 128-bit 128/ln2 (error < 2^-64);
+//   k = rint(+-t), f = +-t - k in [-1/2, 1/2]; r = f ln2/128, held as
+//       r 2^71;
+//   expm1(r) = r + r^2 P(r), P = 1/2 + r/6 + r^2/24 + r^3/120 + r^4/720
+//       (Taylor; the next term is below 2^-72), Horner in Q63;
+//   2^(k/128) = 2^(k >> 7) 2^(j/128), j = k & 127, 2^(j/128) in Q63.
+DUST2_MATH_CORE double exp_fixed(std::uint64_t u) {
+  const std::uint64_t a = u & 0x7fffffffffffffffull;
+  const int be = static_cast<int>(a >> 52);
+  const std::uint64_t mant = (a & 0x000fffffffffffffull) |
+    0x0010000000000000ull;
+  const u128 p_lo = static_cast<u128>(mant) * DUST2_EXP_C120_LO;
+  const u128 p_hi = static_cast<u128>(mant) * DUST2_EXP_C120_HI;
+  const u128 w = p_hi + (p_lo >> 64);  // floor(mant * C / 2^64)
+  const u128 t = w >> (1067 - be);     // |x| 128/ln2 2^64, be in [969, 1032]
+  const u128 tr = t + (static_cast<u128>(1) << 63);
+  const std::int64_t n = static_cast<std::int64_t>(tr >> 64);
+  std::int64_t f = static_cast<std::int64_t>(
+    static_cast<std::uint64_t>(tr) - 0x8000000000000000ull);
+  std::int64_t k = n;
+  if (u >> 63) {
+    k = -n;
+    f = f == INT64_MIN ? INT64_MAX : -f;
+  }
+  // r 2^71 = f ln2 (f in units of 2^-64)
+  const std::int64_t r = static_cast<std::int64_t>(
+    (static_cast<i128>(f) * static_cast<i128>(DUST2_LN2_Q64)) >> 64);
+  std::int64_t pq = 0x002d82d82d82d82ell;          // 1/720 in Q63
+  pq = 0x0111111111111111ll + mul_shift(r, pq, 71);  // 1/120
+  pq = 0x0555555555555555ll + mul_shift(r, pq, 71);  // 1/24
+  pq = 0x1555555555555555ll + mul_shift(r, pq, 71);  // 1/6
+  pq = 0x4000000000000000ll + mul_shift(r, pq, 71);  // 1/2
+  const std::int64_t rp = mul_shift(r, pq, 71);      // r P, Q63
+  const std::int64_t em1 = r + mul_shift(r, rp, 63);  // expm1(r) 2^71
+  const int j = static_cast<int>(k & 127);
+  const int e = static_cast<int>(k >> 7);
+  const std::uint64_t tj = DUST2_TAB(exp2_q63, j);
+  const std::uint64_t v = static_cast<std::uint64_t>(
+    static_cast<i128>(tj) + ((static_cast<i128>(tj) *
+                              static_cast<i128>(em1)) >> 71));
+  // v = 2^(j/128) exp(r) in Q63, in [2^63 - 2^55, 2^64)
+  std::uint64_t m;
+  int ee = e;
+  if (v >> 63) {
+    m = (v >> 11) + ((v >> 10) & 1);
+  } else {
+    m = (v >> 10) + ((v >> 9) & 1);
+    ee -= 1;
+  }
+  if (m >> 53) {
+    m >>= 1;
+    ee += 1;
+  }
+  return from_bits((static_cast<std::uint64_t>(ee + 1023) << 52) |
+                   (m & 0x000fffffffffffffull));
+}
+
+// log(x) for x positive, normal and finite: the method of log() below
+// (x = 2^e m, m in [sqrt(2)/2, sqrt(2)), F = j/256 nearest m,
+// r = (m - F)/F, log x = e ln2 + log F + log1p(r)) in fixed point:
+// r 2^71 from (m - F) and 256/j in Q62; log1p(r) = r Q(r),
+// Q = 1 - r/2 + r^2/3 - ... + r^6/7 in Q62 (the next term of log1p is
+// below 2^-71); the sum at 2^-96, or, for m rounding to F = 1 with e = 0,
+// r Q alone, which keeps full relative precision for x near 1.
+DUST2_MATH_CORE double log_fixed(std::uint64_t u, int e_adj) {
+  const std::uint64_t mant = u & 0x000fffffffffffffull;
+  int e = static_cast<int>(u >> 52) - 1023 + e_adj;
+  const bool half = mant > (0x3ff6a09e667f3bcdull & 0x000fffffffffffffull);
+  const int s = half ? 45 : 44;
+  const std::uint64_t q =
+    (mant + (1ull << (s - 1)) - 1 + ((mant >> s) & 1)) >> s;
+  const std::int64_t m2 = static_cast<std::int64_t>(mant |
+                                                    0x0010000000000000ull);
+  int j;
+  std::int64_t fi;  // m - F in units of 2^-52 (2^-53 when half)
+  if (half) {
+    e += 1;
+    j = 128 + static_cast<int>(q);
+    fi = m2 - (static_cast<std::int64_t>(j) << 45);
+  } else {
+    j = 256 + static_cast<int>(q);
+    fi = m2 - (static_cast<std::int64_t>(j) << 44);
+  }
+  const int i = j - DUST2_LOG_J0;
+  const std::int64_t inv = static_cast<std::int64_t>(
+    DUST2_TAB(log_inv_q62, i));
+  const std::int64_t r = mul_shift(fi, inv, half ? 44 : 43);  // r 2^71
+  std::int64_t pq = 0x0924924924924925ll;               // 1/7 in Q62
+  pq = -0x0aaaaaaaaaaaaaabll + mul_shift(r, pq, 71);    // -1/6
+  pq = 0x0ccccccccccccccdll + mul_shift(r, pq, 71);     // 1/5
+  pq = -0x1000000000000000ll + mul_shift(r, pq, 71);    // -1/4
+  pq = 0x1555555555555555ll + mul_shift(r, pq, 71);     // 1/3
+  pq = -0x2000000000000000ll + mul_shift(r, pq, 71);    // -1/2
+  pq = 0x4000000000000000ll + mul_shift(r, pq, 71);     // Q, Q62
+  const i128 rq = static_cast<i128>(r) * static_cast<i128>(pq);  // 2^-133
+  if (e == 0 && j == 256) {
+    if (rq == 0) {
+      return 0.0;
+    }
+    return rq < 0 ? u128_to_double(static_cast<u128>(-rq), 133, true) :
+      u128_to_double(static_cast<u128>(rq), 133, false);
+  }
+  const i128 ln2 = (static_cast<i128>(DUST2_LN2_96_HI) << 64) |
+    static_cast<i128>(DUST2_LN2_96_LO);
+  const i128 lf = static_cast<i128>(static_cast<u128>(
+    static_cast<std::uint64_t>(DUST2_TAB(log_f96_hi, i))) << 64) |
+    static_cast<i128>(DUST2_TAB(log_f96_lo, i));
+  const i128 sum = static_cast<i128>(e) * ln2 + lf + (rq >> 37);
+  return sum < 0 ? u128_to_double(static_cast<u128>(-sum), 96, true) :
+    u128_to_double(static_cast<u128>(sum), 96, false);
+}
+
 DUST2_HD double exp(double x) {
-  if ((bits_of(x) & 0x7fffffffffffffffull) >= EXP_FAST_BITS) {
+  const std::uint64_t u = bits_of(x);
+  const std::uint64_t a = u & 0x7fffffffffffffffull;
+  if (a >= EXP_FAST_BITS) {
     return exp_slow(x);  // NaN, infinities, |x| >= 704
   }
-  // k = rint(x * 128/ln2), |k| < 2^17, read from the shifted sum's bits
-  const double shifted = x * DUST2_INV_LN2_128 + ROUND_SHIFTER;
-  const double kf = shifted - ROUND_SHIFTER;
-  const int k = static_cast<int>(static_cast<std::uint32_t>(bits_of(shifted)));
-  double r = std::fma(-kf, DUST2_LN2_128_HI, x);
-  r = std::fma(-kf, DUST2_LN2_128_LO, r);
-  const int j = k & 127;
-  const int e = k >> 7;  // (k - j) / 128, exact
-  // expm1(r) = r + r^2 (1/2 + r (1/6 + r (1/24 + r / 120)))
-  double p = std::fma(r, 0x1.1111111111111p-7, 0x1.5555555555555p-5);
-  p = std::fma(p, r, 0x1.5555555555555p-3);
-  p = std::fma(p, r, 0.5);
-  const double pm1 = std::fma(r * r, p, r);
-  const double t_hi = DUST2_TAB(exp2_hi, j);
-  const double t_lo = DUST2_TAB(exp2_lo, j);
-  // v in [2^(-1/256), 2); v * 2^e is normal for |e| <= 1016, so the
-  // product is the exponent add below
-  const double v = t_hi + std::fma(t_hi, pm1, t_lo);
-  return from_bits(bits_of(v) + (static_cast<std::uint64_t>(
-                                   static_cast<std::int64_t>(e)) << 52));
+  if (a < 0x3c90000000000000ull) {
+    return 1.0;  // |x| < 2^-54: 1 + x rounds to 1
+  }
+  return exp_fixed(u);
 }
 
 DUST2_HD double log(double x) {
@@ -254,41 +437,7 @@ DUST2_HD double log(double x) {
     u = bits_of(x * 0x1p54);
     e_adj = -54;
   }
-  const std::uint64_t mant = u & 0x000fffffffffffffull;
-  int e = static_cast<int>(u >> 52) - 1023 + e_adj;
-  // m = 1.mant; if m > sqrt(2) use m / 2 (compare the mantissa bits)
-  const bool half = mant > (0x3ff6a09e667f3bcdull & 0x000fffffffffffffull);
-  // j = rint(256 m) from the mantissa bits (ties to even), and j / 256
-  // assembled as a double; m - j/256 is then exact
-  const int s = half ? 45 : 44;
-  const std::uint64_t q =
-    (mant + (1ull << (s - 1)) - 1 + ((mant >> s) & 1)) >> s;
-  int j;
-  double m, jd;
-  if (half) {
-    e += 1;
-    j = 128 + static_cast<int>(q);
-    m = from_bits(mant | 0x3fe0000000000000ull);
-    jd = from_bits(0x3fe0000000000000ull + (q << 45));
-  } else {
-    j = 256 + static_cast<int>(q);
-    m = from_bits(mant | 0x3ff0000000000000ull);
-    jd = from_bits(0x3ff0000000000000ull + (q << 44));
-  }
-  const double f = m - jd;  // exact
-  const int i = j - DUST2_LOG_J0;
-  const double r = f * DUST2_TAB(log_inv, i);
-  // log1p(r) = r + r^2 (-1/2 + r (1/3 + r (-1/4 + r (1/5 + r (-1/6 + r/7)))))
-  double p = std::fma(r, 0x1.2492492492492p-3, -0x1.5555555555555p-3);
-  p = std::fma(p, r, 0x1.999999999999ap-3);
-  p = std::fma(p, r, -0.25);
-  p = std::fma(p, r, 0x1.5555555555555p-2);
-  p = std::fma(p, r, -0.5);
-  const double lp = std::fma(r * r, p, r);
-  const double ef = static_cast<double>(e);
-  const double hi = std::fma(ef, LN2_HI, DUST2_TAB(log_hi, i));
-  const double lo = std::fma(ef, LN2_LO, DUST2_TAB(log_lo, i)) + lp;
-  return hi + lo;
+  return log_fixed(u, e_adj);
 }
 
 DUST2_HD float float_from_bits(std::uint32_t u) {

@@ -4,7 +4,8 @@ kernels and the CPU oracle (dust2_gb300/csrc/dust2gpu/).
 * Streams: checked against an independent numpy implementation of
   xoshiro256+ / SplitMix64 / jump (tests/xoshiro.py), including the GF(2)
   skip-ahead the engine uses to seed large stream blocks in parallel.
-* Elementary functions: checked against numpy/scipy within a few ulp.
+* Elementary functions: checked against numpy/scipy within a few ulp,
+  and exp/log against 50-digit decimal arithmetic within 0.51 ulp.
 * Samplers: checked for their distribution (mean, variance, chi-square
   against the exact pmf) on the host build; the GPU tests check that the
   device draws are bit-identical to these.
@@ -83,6 +84,43 @@ def test_exp_log_accuracy(built):
     assert pyoracle.port_math("log", np.array([1.0]))[0] == 0
     assert pyoracle.port_math("log", np.array([0.0]))[0] == -np.inf
     assert np.isnan(pyoracle.port_math("log", np.array([-1.0]))[0])
+
+
+def _ulps_exact(got, exact):
+    """Distance of each double in got from the exact Decimal value, in
+    ulps of the correctly rounded result."""
+    from decimal import Decimal
+    out = []
+    for g, e in zip(got, exact):
+        sp = Decimal(float(np.spacing(abs(float(e)))))
+        out.append(float(abs(Decimal(float(g)) - e) / sp))
+    return np.array(out)
+
+
+def test_exp_log_fixed_point_accuracy(built):
+    """The integer fixed-point exp and log against 50-digit decimal
+    arithmetic: within 0.51 ulp (nearly always correctly rounded),
+    including arguments near 1 for log and near the ends of exp's
+    fixed-point range."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 50
+    rs = np.random.default_rng(7)
+    x = np.concatenate([rs.uniform(-703, 703, 1500), rs.uniform(-1, 1, 500),
+                        np.exp(rs.uniform(-36, -7, 300)) *
+                        rs.choice([-1, 1], 300),
+                        [2.0 ** -54, -(2.0 ** -53), 703.99, -703.99]])
+    e = pyoracle.port_math("exp", x)
+    u = _ulps_exact(e, [Decimal(float(v)).exp() for v in x])
+    assert u.max() <= 0.51
+    y = np.concatenate([np.exp(rs.uniform(-700, 700, 1000)),
+                        1 + rs.uniform(-1e-3, 1e-3, 500),
+                        1 + np.exp(rs.uniform(-36, -10, 300)) *
+                        rs.choice([-1, 1], 300),
+                        [5e-324, 2.2250738585072014e-308,
+                         1.7976931348623157e308, 0.5, 2.0]])
+    ly = pyoracle.port_math("log", y)
+    u = _ulps_exact(ly, [Decimal(float(v)).ln() for v in y])
+    assert u.max() <= 0.51
 
 
 def test_lgamma_accuracy(built):
