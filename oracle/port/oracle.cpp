@@ -1424,7 +1424,7 @@ int oracle_mixed_simulate(const char* name, const double* pars, int n_groups,
 }
 
 // The project's elementary functions evaluated on the host (fn: 0 exp,
-// 1 log, 2 lgamma, 3 cos(2 pi x), 4 sin(2 pi x)).
+// 1 log, 2 lgamma, 3 cos(2 pi x), 4 sin(2 pi x), 5 rcp).
 void oracle_math(int fn, const double* x, int n, double* out) {
   for (int i = 0; i < n; ++i) {
     double s, c;
@@ -1433,6 +1433,7 @@ void oracle_math(int fn, const double* x, int n, double* out) {
     case 1: out[i] = dust2gpu::math::log(x[i]); break;
     case 2: out[i] = dust2gpu::math::lgamma(x[i]); break;
     case 3: dust2gpu::math::sincos_2pi(x[i], &s, &c); out[i] = c; break;
+    case 5: out[i] = dust2gpu::math::rcp(x[i]); break;
     default: dust2gpu::math::sincos_2pi(x[i], &s, &c); out[i] = s; break;
     }
   }

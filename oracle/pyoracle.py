@@ -420,13 +420,15 @@ def ref():
 
 
 def port_math(fn, x):
-    """The project's exp/log/lgamma/cos2pi/sin2pi evaluated on the host."""
+    """The project's exp/log/lgamma/cos2pi/sin2pi/rcp evaluated on the
+    host."""
     o = port()
     x = np.ascontiguousarray(x, dtype=np.float64)
     out = np.empty_like(x)
     f = o.lib.oracle_math
     f.restype = None
-    code = {"exp": 0, "log": 1, "lgamma": 2, "cos2pi": 3, "sin2pi": 4}[fn]
+    code = {"exp": 0, "log": 1, "lgamma": 2, "cos2pi": 3, "sin2pi": 4,
+            "rcp": 5}[fn]
     f(ctypes.c_int(code), x.ctypes.data_as(_d), ctypes.c_int(x.size),
       out.ctypes.data_as(_d))
     return out

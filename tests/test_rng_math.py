@@ -123,6 +123,19 @@ def test_exp_log_fixed_point_accuracy(built):
     assert u.max() <= 0.51
 
 
+def test_rcp(built):
+    """rcp (FP32 seed and two FP64 Newton steps) is within 1 ulp of the
+    IEEE quotient."""
+    rs = np.random.default_rng(4)
+    n = 50000
+    y = np.concatenate([rs.uniform(0.5, 2, n),
+                        np.exp(rs.uniform(-60, 60, n)) *
+                        rs.choice([-1, 1], n),
+                        [1.0, 2.0, 0.5, 3.0, 0.1, np.nextafter(1.0, 2.0),
+                         np.nextafter(2.0, 1.0)]])
+    assert np.max(ulp_err(pyoracle.port_math("rcp", y), 1.0 / y)) <= 1
+
+
 def test_lgamma_accuracy(built):
     x = np.concatenate([np.arange(1, 200, dtype=float),
                         np.random.default_rng(2).uniform(0.01, 1e6, 20000)])
