@@ -64,6 +64,12 @@ DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 1175.8,
                        "ode_batched": 40.0}
 
 
+# The CPU path is timed with the oracle's timing build: the host's libm
+# exp and log, as dust2 evaluates them through monty, in place of the
+# integer fixed-point functions the GPU uses (which are slower on a CPU).
+CPU_MATH = "host libm exp/log (as dust2/monty call them)"
+
+
 def traffic_per_launch(workload, units_per_launch):
     b = DRAM_BYTES_PER_UNIT.get(workload)
     return None if b is None else b * units_per_launch
@@ -226,7 +232,7 @@ def run_cpu(w, n_groups, n_threads, n_runs=1):
     returns (seconds per run, particle-steps per run)."""
     from oracle import pyoracle
     import dust2_gb300 as d
-    port = pyoracle.port()
+    port = pyoracle.port_timing()
     npg = w["n_particles"][:n_groups]
     G_all = len(w["n_particles"])
     gen = d.Generator(w["system"])
@@ -246,7 +252,7 @@ def run_cpu(w, n_groups, n_threads, n_runs=1):
 
 def cpu_baseline(w, target_seconds):
     from oracle import pyoracle
-    port = pyoracle.port()
+    port = pyoracle.port_timing()
     threads = port.max_threads()
     # calibrate on the first group, then grow the sample to the target
     t1, ps1 = run_cpu(w, 1, threads)
@@ -263,7 +269,8 @@ def cpu_baseline(w, target_seconds):
               f" particles), all {w['times'].size} observations, one "
               "likelihood evaluation")
     return {"value": ps / t, "unit": "particle-steps/s", "cores": threads,
-            "kind": "port", "sample": sample, "seconds": t}
+            "kind": "port", "sample": sample, "seconds": t,
+            "math": CPU_MATH}
 
 
 def gpu_simulate_factory():
@@ -627,7 +634,7 @@ def ode_alloc(w, seed=1):
 
 def ode_cpu(w, n_inst, threads):
     from oracle import pyoracle
-    port = pyoracle.port()
+    port = pyoracle.port_timing()
     gen_pars = 4
     pars = np.asarray(w["pars"]).reshape(-1, gen_pars)[:n_inst].ravel()
     t0 = time.perf_counter()
@@ -639,14 +646,14 @@ def ode_cpu(w, n_inst, threads):
 
 def ode_cpu_baseline(w, target_seconds):
     from oracle import pyoracle
-    threads = pyoracle.port().max_threads()
+    threads = pyoracle.port_timing().max_threads()
     n = 1024
     t, steps = ode_cpu(w, n, threads)
     while t < target_seconds / 4 and n < w["n_groups"]:
         n = min(w["n_groups"], n * 4)
         t, steps = ode_cpu(w, n, threads)
     return {"value": steps / t, "unit": "dopri5 steps/s", "cores": threads,
-            "kind": "port",
+            "kind": "port", "math": CPU_MATH,
             "sample": f"instances 1-{n} of {w['n_groups']}, integrated "
                       f"0..200 with {w['times'].size} outputs",
             "seconds": t}
@@ -719,7 +726,10 @@ def ode_arm(args, rank, world, local):
         elapsed.append(e0.elapsed_time(e1))
     clock_info = clocks.stop()
     ms = float(np.mean(elapsed))
-    host = np.empty(n_out)
+    # the caller's output buffer: pinned host memory, as the timing
+    # contract's host<->device copies are
+    host_t = torch.empty(n_out, dtype=torch.float64, pin_memory=True)
+    host = host_t.numpy()
     e2e = []
     for _ in range(args.steps):
         torch.cuda.synchronize()
@@ -777,7 +787,7 @@ def reference_arm(args, rank, world):
     engine_build.build()
     from oracle import pyoracle
 
-    port = pyoracle.port()
+    port = pyoracle.port_timing()
     threads = port.max_threads()
     metric, unit = "filter particle-steps/s", "particle-steps/s"
     if args.workload == "ode_batched":
@@ -823,7 +833,7 @@ def reference_arm(args, rank, world):
         "config": {"workload": args.workload},
         "cpu_baseline": {"value": value, "unit": unit,
                          "cores": threads, "kind": "port",
-                         "sample": base["sample"]},
+                         "sample": base["sample"], "math": CPU_MATH},
         "e2e": {"value": value, "unit": unit,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -835,7 +845,7 @@ def serve_cpu_run(w, clients, threads):
     oracle (the reference's engine restated; OpenMP over particles)."""
     from oracle import pyoracle
     import dust2_gb300 as d
-    port = pyoracle.port()
+    port = pyoracle.port_timing()
     gen = d.Generator("seir_age")
     total = 0
     t0 = time.perf_counter()

@@ -408,6 +408,10 @@ DUST2_MATH_CORE double log_fixed(std::uint64_t u, int e_adj) {
 }
 
 DUST2_HD double exp(double x) {
+#if defined(DUST2_HOST_LIBM) && !defined(__CUDA_ARCH__)
+  // the timing build of the CPU oracle: the host's libm, as dust2 calls it
+  return std::exp(x);
+#endif
   const std::uint64_t u = bits_of(x);
   const std::uint64_t a = u & 0x7fffffffffffffffull;
   if (a >= EXP_FAST_BITS) {
@@ -420,6 +424,9 @@ DUST2_HD double exp(double x) {
 }
 
 DUST2_HD double log(double x) {
+#if defined(DUST2_HOST_LIBM) && !defined(__CUDA_ARCH__)
+  return std::log(x);
+#endif
   std::uint64_t u = bits_of(x);
   int e_adj = 0;
   // positive normal finite numbers have u in [2^52, 0x7ff0...)

@@ -19,6 +19,7 @@ REPO = HERE.parent
 CSRC = REPO / "dust2_gb300" / "csrc"
 PORT_SRC = HERE / "port" / "oracle.cpp"
 PORT_LIB = HERE / "_build" / "liboracle.so"
+PORT_LIBM_LIB = HERE / "_build" / "liboracle_libm.so"
 REF_LIB = HERE / "_ref" / "libdust2_ref.so"
 REF_INCLUDE = Path(os.environ.get("DUST2_REF",
                                   "/root/reference/inst/include"))
@@ -30,20 +31,27 @@ def _inputs():
             [CSRC / "engine" / "error_text.hpp", Path(__file__)])
 
 
-def build_port(force=False):
+def build_port(force=False, libm=False):
+    """The CPU restatement.  libm=True builds the timing variant, which
+    evaluates exp and log with the host's libm as dust2 does (through
+    monty) instead of the project's bit-exact functions: it times the CPU
+    path as the reference runs it, and is never used as a checker."""
+    lib = PORT_LIBM_LIB if libm else PORT_LIB
     newest = max(p.stat().st_mtime for p in _inputs())
-    if not force and PORT_LIB.exists() and PORT_LIB.stat().st_mtime >= newest:
-        return PORT_LIB
-    PORT_LIB.parent.mkdir(exist_ok=True)
-    tmp = PORT_LIB.with_suffix(".so.tmp")
+    if not force and lib.exists() and lib.stat().st_mtime >= newest:
+        return lib
+    lib.parent.mkdir(exist_ok=True)
+    tmp = lib.with_suffix(".so.tmp")
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared",
-           "-ffp-contract=off", "-fno-strict-aliasing", "-I", str(CSRC),
-           str(PORT_SRC), "-o", str(tmp)]
+           "-ffp-contract=off", "-fno-strict-aliasing", "-I", str(CSRC)]
+    if libm:
+        cmd.append("-DDUST2_HOST_LIBM")
+    cmd += [str(PORT_SRC), "-o", str(tmp)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, PORT_LIB)
-    return PORT_LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 def build_ref(force=False):

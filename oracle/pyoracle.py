@@ -407,6 +407,19 @@ def port():
     return _port
 
 
+_port_timing = None
+
+
+def port_timing():
+    """The timing build of the restatement (host libm exp and log, as
+    dust2 evaluates them): for timing the CPU path only."""
+    global _port_timing
+    if _port_timing is None:
+        from . import build
+        _port_timing = Oracle(build.build_port(libm=True), "port")
+    return _port_timing
+
+
 def ref():
     """dust2's own engine, or None where the reference build is absent."""
     global _ref
