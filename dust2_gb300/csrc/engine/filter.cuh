@@ -78,7 +78,7 @@ struct filter_view {
   double* w;                  // [n_total] raw log weights
   double* ew;                 // [n_total] exp(w - max)
   double* pre;                // [n_total] tile-local inclusive prefix
-  double* chunk_sum;          // [n_chunks] chunk totals of ew
+  double* chunk_sum;          // [n_chunks] chunk totals of ew (ends after k_group)
   double* chunk_off;          // [n_chunks] exclusive offsets within group
   unsigned long long* gkey;   // [n_groups] ordered key of max log weight
   int* gnz;                   // [n_groups] any weight != 0
@@ -246,6 +246,8 @@ DUST2_PARTICLE_KERNEL(T) k_step_compare(system_view<T> v, filter_view f,
 // Exclusive offsets of a group's chunks (warp scans of 32 chunk totals
 // and a running carry; the exclusive value comes from the neighbour
 // lane, so every offset is a plain sum); returns the group total.
+// Afterwards chunk_sum holds each chunk's end, offset + total (the value
+// the resampling search compares with, computed once here).
 __device__ __forceinline__ double group_chunk_offsets(const filter_view& f,
                                                       int g, int lane) {
   const int c0 = f.chunk_first[g];
@@ -260,7 +262,9 @@ __device__ __forceinline__ double group_chunk_offsets(const filter_view& f,
       excl = 0;
     }
     if (c < nc) {
-      f.chunk_off[c0 + c] = carry + excl;
+      const double off = carry + excl;
+      f.chunk_off[c0 + c] = off;
+      f.chunk_sum[c0 + c] = off + v;
     }
     carry = carry + __shfl_sync(0xffffffffu, incl, 31);
   }

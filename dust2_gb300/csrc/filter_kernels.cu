@@ -137,13 +137,15 @@ __global__ void k_resample(filter_view f) {
   const int n = f.n_particles[g];
   const int i = tl.local + threadIdx.x;
   const double uu = f.guu0[g] + static_cast<double>(i) * f.gdu[g];
-  // first chunk whose last prefix reaches uu
+  // first chunk whose last prefix (its end, left in chunk_sum by k_group)
+  // reaches uu; every value compared is >= +0, so the comparisons are
+  // taken on the bits
   const int c0 = f.chunk_first[g];
   const int nc = f.chunk_count[g];
   int lo = 0, hi = nc;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
-    if (f.chunk_off[c0 + mid] + f.chunk_sum[c0 + mid] >= uu) {
+    if (math::le_nonneg(uu, f.chunk_sum[c0 + mid])) {
       hi = mid;
     } else {
       lo = mid + 1;
@@ -160,7 +162,7 @@ __global__ void k_resample(filter_view f) {
     const double* pre = f.pre + f.offset[g];
     while (a < b) {
       const int mid = (a + b) >> 1;
-      if (off + pre[mid] >= uu) {
+      if (math::le_nonneg(uu, off + pre[mid])) {
         b = mid;
       } else {
         a = mid + 1;
@@ -260,7 +262,7 @@ __global__ void k_fallback_count(filter_view f, int* count) {
     int a = 0, b = n;  // first m with ser[m] >= uu, or n
     while (a < b) {
       const int mid = (a + b) >> 1;
-      if (ser[mid] >= uu) {
+      if (math::le_nonneg(uu, ser[mid])) {
         b = mid;
       } else {
         a = mid + 1;
