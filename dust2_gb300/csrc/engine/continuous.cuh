@@ -440,13 +440,55 @@ public:
                             n_index_state * sizeof(int),
                             cudaMemcpyHostToDevice));
     }
-    device_array<double> buf(static_cast<std::size_t>(L.n_total) * n_out *
-                             n_times);
-    launch_run(times, n_times, buf.data(), idx.data(), n_out);
-    DUST2_CUDA(cudaMemcpyAsync(out, buf.data(), buf.size() * sizeof(double),
-                               cudaMemcpyDeviceToHost, base_.stream()));
+    // The output times are integrated in up to 8 consecutive launches
+    // (each continuing from the last one's state and solver record, so the
+    // result is that of one launch), all enqueued first; each chunk of
+    // outputs is then copied to the host on a second stream as soon as its
+    // launch is done, while the next chunk integrates.
+    const std::size_t per_time = static_cast<std::size_t>(L.n_total) * n_out;
+    if (sim_buf_.size() < per_time * n_times) {
+      sim_buf_.resize(per_time * n_times);
+    }
+    if (copy_stream_ == nullptr) {
+      DUST2_CUDA(cudaStreamCreateWithFlags(&copy_stream_,
+                                           cudaStreamNonBlocking));
+      for (auto& e : chunk_done_) {
+        DUST2_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      }
+    }
+    const int n_chunks = std::min(n_times, n_sim_chunks);
+    std::vector<int> first(n_chunks + 1);
+    for (int c = 0; c <= n_chunks; ++c) {
+      first[c] = static_cast<int>(static_cast<long>(n_times) * c / n_chunks);
+    }
+    for (int c = 0; c < n_chunks; ++c) {
+      if (c > 0) {
+        base_.set_time(times[first[c] - 1]);
+      }
+      launch_run(times + first[c], first[c + 1] - first[c],
+                 sim_buf_.data() + first[c] * per_time, idx.data(), n_out);
+      DUST2_CUDA(cudaEventRecord(chunk_done_[c], base_.stream()));
+    }
+    for (int c = 0; c < n_chunks; ++c) {
+      DUST2_CUDA(cudaStreamWaitEvent(copy_stream_, chunk_done_[c], 0));
+      DUST2_CUDA(cudaMemcpyAsync(
+        out + first[c] * per_time, sim_buf_.data() + first[c] * per_time,
+        (first[c + 1] - first[c]) * per_time * sizeof(double),
+        cudaMemcpyDeviceToHost, copy_stream_));
+    }
+    DUST2_CUDA(cudaStreamSynchronize(copy_stream_));
     base_.check_errors_after();
     base_.set_time(times[n_times - 1]);
+  }
+
+  ~continuous_system() override {
+    if (copy_stream_ != nullptr) {
+      cudaStreamSynchronize(copy_stream_);
+      for (auto e : chunk_done_) {
+        cudaEventDestroy(e);
+      }
+      cudaStreamDestroy(copy_stream_);
+    }
   }
 
   // Run through `times` leaving outputs in a caller-provided device
@@ -691,6 +733,11 @@ private:
   device_array<int> requires_init_dev_;
   device_array<double> times_dev_;
   device_array<double> other_;
+  // simulate(): output buffer and the stream its chunks are copied on
+  static constexpr int n_sim_chunks = 8;
+  device_array<double> sim_buf_;
+  cudaStream_t copy_stream_ = nullptr;
+  cudaEvent_t chunk_done_[n_sim_chunks] = {};
 };
 
 }  // namespace engine
