@@ -1,6 +1,7 @@
 """Generate dust2gpu/tables.hpp: correctly rounded constant tables for the
-table-driven exp and log of math.hpp and the reciprocals of small
-integers used by the binomial inversion sampler.
+table-driven exp and log of math.hpp (double tables for exp's FP64 slow
+path, fixed-point tables for the integer exp and log) and the reciprocals
+of small integers used by the binomial inversion sampler.
 
 Every value is computed in 60-digit decimal arithmetic and rounded once to
 the nearest double; a "lo" entry holds the rounded remainder of the exact
@@ -53,27 +54,12 @@ def main():
     out.append("#define DUST2_EXP2_LO \\")
     out.append(",\\\n".join("  " + ", ".join(fmt(v) for v in los[i:i + 3])
                            for i in range(0, 128, 3)))
-    # log: F = j/256 for j = 181..363 (m in [sqrt(2)/2, sqrt(2)))
+    # log: F = j/256 for j = 181..363 (m in [sqrt(2)/2, sqrt(2))); the
+    # fixed-point tables are written by fixed_point_tables()
     out.append("")
-    out.append("// For F = j/256, j = LOG_J0 + i: 1/F (rounded) and")
-    out.append("// log(F) = LOG_HI[i] + LOG_LO[i]")
     j0, j1 = 181, 363
     out.append(f"#define DUST2_LOG_J0 {j0}")
     out.append(f"#define DUST2_LOG_N {j1 - j0 + 1}")
-    inv, lhi, llo = [], [], []
-    for j in range(j0, j1 + 1):
-        F = Fraction(j, 256)
-        inv.append(rn(1 / F))
-        v = (Decimal(j) / Decimal(256)).ln()
-        h, lo = hi_lo(v)
-        lhi.append(h)
-        llo.append(lo)
-    for name, vals in (("DUST2_LOG_INV", inv), ("DUST2_LOG_HI", lhi),
-                       ("DUST2_LOG_LO", llo)):
-        out.append(f"#define {name} \\")
-        out.append(",\\\n".join(
-            "  " + ", ".join(fmt(v) for v in vals[i:i + 3])
-            for i in range(0, len(vals), 3)))
     # 1/x for x = 0..128 (entry 0 unused)
     out.append("")
     out.append("// 1/x, x = 0..128 (entry 0 is 0)")
