@@ -60,7 +60,7 @@ FP64_PIPE_INST_PER_UNIT = {"sir_batched": 162.7, "seir_batched": 2682.7,
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
 # same kernel, from the same captures; `traffic` is this times the units
 # of one launch.
-DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 1175.8,
+DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2653.4,
                        "ode_batched": 40.0}
 
 

@@ -18,6 +18,9 @@ namespace systems {
 
 struct seir_age {
   static constexpr const char* name = "seir_age";
+  // kernels of this system fit 3 blocks of 128 threads per SM (170
+  // registers): measured 2.6% faster than 2 blocks (255 registers)
+  static constexpr int min_blocks_per_sm = 3;
   using real_type = double;
   using rng_state_type = random::rng_state;
   static constexpr int n_age = 16;
