@@ -440,7 +440,11 @@ def gpu_arm(args, rank, world, local):
             "e2e": {"value": particle_steps * world / e2e_max,
                     "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_max},
-            "gpu_launches": args.steps * (2 + 6 * n_obs),
+            # per observation: the step kernel and the tail, which is one
+            # cluster launch when every group has <= 1024 particles, else
+            # weights, group, resample, fallback and reorder
+            "gpu_launches": args.steps * (
+                2 + (2 if max(npg) <= 1024 else 6) * n_obs),
             "clocks": clock_info,
             "roofline": roofline,
             "serial_fallbacks": d.dust_likelihood_serial_fallbacks(obj),

@@ -127,6 +127,8 @@ _SIGNATURES = {
         c_double_p, ctypes.c_size_t, c_double_p]),
     "dust2_gb300_filter_set_serial_resample": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32]),
+    "dust2_gb300_filter_set_fused_tail": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32]),
     "dust2_gb300_filter_run_async": (ctypes.c_int, [
         ctypes.c_void_p, c_size_p, ctypes.c_size_t]),
     "dust2_gb300_filter_last_log_likelihood": (ctypes.c_int, [

@@ -959,6 +959,11 @@ int dust2_gb300_filter_set_serial_resample(dust2_gb300_filter* filter,
   return guard([&] { filref(filter).set_serial_resample(serial != 0); });
 }
 
+int dust2_gb300_filter_set_fused_tail(dust2_gb300_filter* filter,
+                                      int32_t fused) {
+  return guard([&] { filref(filter).set_fused_tail(fused != 0); });
+}
+
 int dust2_gb300_filter_run_async(dust2_gb300_filter* filter,
                                  const size_t* index_group,
                                  size_t n_index_group) {

@@ -130,6 +130,10 @@ public:
   virtual void set_use_graph(bool use) = 0;
   // Resample every group with the serial algorithm (verification mode).
   virtual void set_serial_resample(bool serial) = 0;
+  // Run the per-observation tail of filters whose groups all have at most
+  // 1024 particles as one launch (default) or as separate kernels; both
+  // give the same results.
+  virtual void set_fused_tail(bool fused) = 0;
   // Enqueue a run on the filter's stream without waiting; the
   // log-likelihood stays on the device until last_log_likelihood().
   virtual void run_async(const int* index_group, int n_index_group) = 0;

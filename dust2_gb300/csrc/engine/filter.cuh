@@ -274,6 +274,13 @@ __device__ __forceinline__ double group_chunk_offsets(const filter_view& f,
 __global__ void k_weights(filter_view f);
 __global__ void k_group(filter_view f, int n_groups);
 __global__ void k_resample(filter_view f);
+// The one-launch tail: a cluster of TAIL_CLUSTER blocks of TAIL_BLOCK
+// threads per group, for groups of at most TAIL_MAX_PARTICLES.
+constexpr int TAIL_CLUSTER = 8;
+constexpr int TAIL_BLOCK = 128;
+constexpr int TAIL_MAX_PARTICLES = TAIL_CLUSTER * TAIL_BLOCK;
+__global__ void k_tail_cluster(filter_view f, int* count, const double* src,
+                               double* dst, int stride, int n_state);
 __global__ void k_save_history(const double* state, int stride,
                                const int* index_state, int n_save,
                                const tile* tiles, const int* active,
@@ -376,6 +383,7 @@ public:
                                cudaMemcpyHostToDevice, s));
     put_rng_state(rng_words.data());
     sys_->sync();
+    set_fused_tail(true);
   }
 
   system_api& sys() override {
@@ -395,6 +403,18 @@ public:
   }
   void set_use_graph(bool use) override {
     use_graph_ = use;
+  }
+
+  void set_fused_tail(bool fused) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    int n_max = 0;
+    for (int n : sys_->layout().n_particles) {
+      n_max = std::max(n_max, n);
+    }
+    fused_tail_ = fused && n_max <= TAIL_MAX_PARTICLES;
+    graph_state_ptr_ = nullptr;  // force a re-capture
   }
 
   void set_serial_resample(bool serial) override {
@@ -860,13 +880,19 @@ private:
       if (timing_) {
         record(ev_step_[2 * i + 1]);
       }
-      k_weights<<<NT, TS, 0, s>>>(f);
-      k_group<<<G, 32, 0, s>>>(f, G);
-      k_resample<<<NT, TS, 0, s>>>(f);
-      k_fallback_counted(f, s);
-      k_reorder<<<NT, TS, 0, s>>>(cur, other, L.stride, S.n_state(),
-                                  L.tiles.empty() ? nullptr : S.tiles_dev(),
-                                  offset_.data(), idx_.data(), mode_.data());
+      if (fused_tail_) {
+        k_tail_cluster<<<G * TAIL_CLUSTER, TAIL_BLOCK, 0, s>>>(
+          f, fallback_count_.data(), cur, other, L.stride, S.n_state());
+      } else {
+        k_weights<<<NT, TS, 0, s>>>(f);
+        k_group<<<G, 32, 0, s>>>(f, G);
+        k_resample<<<NT, TS, 0, s>>>(f);
+        k_fallback_counted(f, s);
+        k_reorder<<<NT, TS, 0, s>>>(cur, other, L.stride, S.n_state(),
+                                    L.tiles.empty() ? nullptr :
+                                    S.tiles_dev(), offset_.data(),
+                                    idx_.data(), mode_.data());
+      }
       if constexpr (is_continuous<T>()) {
         owner_->enqueue_reorder_record(S.tiles_dev(), NT, TS, offset_.data(),
                                        idx_.data(), mode_.data(), s);
@@ -983,6 +1009,7 @@ private:
   std::vector<int> random_particle_;
   bool has_run_ = false;
   bool use_graph_ = true;
+  bool fused_tail_ = false;  // k_tail_cluster instead of separate kernels
   bool pending_ = false;
   bool capturing_ = false;
   bool timing_ = false;

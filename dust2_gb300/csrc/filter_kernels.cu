@@ -4,6 +4,8 @@
 #include <cfloat>
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "dust2gpu/math.hpp"
 #include "dust2gpu/random.hpp"
 #include "engine/device.cuh"
@@ -30,6 +32,14 @@ __global__ void k_filter_reset(filter_view f, int n_groups) {
 // scans of 32 chunks with a running carry.  The log-likelihood and the
 // resampling indices are therefore the same for any tile size.
 
+// A particle's weight relative to the group's largest, exp(w - max); a
+// NaN log weight counts as weight 0.
+__device__ __forceinline__ double scaled_weight(const filter_view& f, int k,
+                                                double mx) {
+  const double w = f.w[k];
+  return (w != w) ? 0.0 : math::exp(w - mx);
+}
+
 // exp(w - max), the chunk-local inclusive prefix sums and chunk totals.
 __global__ void k_weights(filter_view f) {
   const tile tl = f.tiles[blockIdx.x];
@@ -47,11 +57,7 @@ __global__ void k_weights(filter_view f) {
   }
   const bool valid = static_cast<int>(threadIdx.x) < tl.count;
   const int k = tl.start + threadIdx.x;
-  double e = 0;
-  if (valid) {
-    const double w = f.w[k];
-    e = (w != w) ? 0.0 : math::exp(w - mx);
-  }
+  const double e = valid ? scaled_weight(f, k, mx) : 0.0;
   const double incl = warp_inclusive_scan(e);
   if (valid) {
     f.ew[k] = e;
@@ -62,14 +68,9 @@ __global__ void k_weights(filter_view f) {
   }
 }
 
-// One warp per group: chunk offsets, log-likelihood increment and the
-// resampling uniform; then clear the per-observation reductions.
-__global__ void k_group(filter_view f, int n_groups) {
-  const int g = blockIdx.x;
-  const int lane = threadIdx.x;
-  if (g >= n_groups || !f.active[g]) {
-    return;
-  }
+// One warp of a running group: chunk offsets, log-likelihood increment
+// and the resampling uniform; then clear the per-observation reductions.
+__device__ void group_update(const filter_view& f, int g, int lane) {
   const int n = f.n_particles[g];
   const bool nz = f.gnz[g] != 0;
   const double mx = ordered_value(f.gkey[g]);
@@ -113,29 +114,25 @@ __global__ void k_group(filter_view f, int n_groups) {
   }
 }
 
+__global__ void k_group(filter_view f, int n_groups) {
+  const int g = blockIdx.x;
+  if (g >= n_groups || !f.active[g]) {
+    return;
+  }
+  group_update(f, g, threadIdx.x);
+}
+
 // Prefix sum Q_m (weights 0..m of the group) for group-local index m.
 __device__ __forceinline__ double prefix_at(const filter_view& f, int g,
                                             int m) {
   return f.chunk_off[f.chunk_first[g] + (m >> 5)] + f.pre[f.offset[g] + m];
 }
 
-__global__ void k_resample(filter_view f) {
-  const tile tl = f.tiles[blockIdx.x];
-  const int g = tl.group;
-  if (!f.active[g]) {
-    return;
-  }
-  const int mode = f.mode[g];
-  if (mode == MODE_KEEP || static_cast<int>(threadIdx.x) >= tl.count) {
-    return;
-  }
-  const int k = tl.start + threadIdx.x;
-  if (mode == MODE_FIRST) {
-    f.idx[k] = 0;
-    return;
-  }
+// The resampling index of particle i (global index k) of a group being
+// resampled; an ambiguous decision is recorded in *flag.
+__device__ void resample_particle(const filter_view& f, int g, int i, int k,
+                                  int* flag) {
   const int n = f.n_particles[g];
-  const int i = tl.local + threadIdx.x;
   const double uu = f.guu0[g] + static_cast<double>(i) * f.gdu[g];
   // first chunk whose last prefix (its end, left in chunk_sum by k_group)
   // reaches uu; every value compared is >= +0, so the comparisons are
@@ -202,8 +199,26 @@ __global__ void k_resample(filter_view f) {
   }
   f.idx[k] = m;
   if (!ok) {
-    atomicOr(f.gflag + g, 1);
+    atomicOr(flag, 1);
   }
+}
+
+__global__ void k_resample(filter_view f) {
+  const tile tl = f.tiles[blockIdx.x];
+  const int g = tl.group;
+  if (!f.active[g]) {
+    return;
+  }
+  const int mode = f.mode[g];
+  if (mode == MODE_KEEP || static_cast<int>(threadIdx.x) >= tl.count) {
+    return;
+  }
+  const int k = tl.start + threadIdx.x;
+  if (mode == MODE_FIRST) {
+    f.idx[k] = 0;
+    return;
+  }
+  resample_particle(f, g, tl.local + threadIdx.x, k, f.gflag + g);
 }
 
 // The reference algorithm (filter_details.hpp:45-74) for groups with an
@@ -216,13 +231,10 @@ __global__ void k_resample(filter_view f) {
 // binary search.  The serial sums overwrite this group's `pre` entries.
 constexpr int FALLBACK_CHUNK = 2048;
 
-__global__ void k_fallback_count(filter_view f, int* count) {
+// The whole block resamples group g serially and counts it.
+__device__ void serial_fallback(const filter_view& f, int g, int* count) {
   __shared__ double buf[FALLBACK_CHUNK];
   __shared__ double total;
-  const int g = blockIdx.x;
-  if (!f.active[g] || f.mode[g] != MODE_RESAMPLE || !f.gflag[g]) {
-    return;
-  }
   const int n = f.n_particles[g];
   const double* w = f.ew + f.offset[g];
   double* ser = f.pre + f.offset[g];
@@ -269,6 +281,89 @@ __global__ void k_fallback_count(filter_view f, int* count) {
       }
     }
     idx[i] = a == n ? n - 1 : a;
+  }
+}
+
+__global__ void k_fallback_count(filter_view f, int* count) {
+  const int g = blockIdx.x;
+  if (!f.active[g] || f.mode[g] != MODE_RESAMPLE || !f.gflag[g]) {
+    return;
+  }
+  serial_fallback(f, g, count);
+}
+
+// The tail of an observation for groups of at most TAIL_MAX_PARTICLES
+// particles, as one launch: k_weights, k_group, k_resample,
+// k_fallback_count and k_reorder.  Each group is a cluster of
+// TAIL_CLUSTER blocks (warp w of block r holds the group's chunk
+// 4r + w), so the FP64 work of the group is spread over the FP64 units of
+// TAIL_CLUSTER SMs, one warp per SM partition, and the phases are
+// separated by cluster barriers, whose release/acquire semantics make the
+// global writes of one phase visible to the next.  Every value is
+// computed by the same device functions in the same order as by the
+// separate kernels, so the results are the same bits.  Every block of a
+// running group takes all four barriers whatever the data, so no barrier
+// can wait for a block that has left.  The state of every group moves
+// from src to dst (in place for groups that keep their particles), as
+// k_reorder does.
+__global__ void __cluster_dims__(TAIL_CLUSTER, 1, 1)
+__launch_bounds__(TAIL_BLOCK)
+k_tail_cluster(filter_view f, int* count, const double* __restrict__ src,
+               double* __restrict__ dst, int stride, int n_state) {
+  __shared__ int flag;  // ambiguous decisions, used in block rank 0
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int g = blockIdx.x / TAIL_CLUSTER;
+  const int rank = static_cast<int>(cluster.block_rank());
+  const int i = rank * TAIL_BLOCK + static_cast<int>(threadIdx.x);
+  const int n = f.n_particles[g];
+  const int base = f.offset[g];
+  if (f.active[g]) {
+    if (threadIdx.x == 0) {
+      flag = 0;
+    }
+    const double mx = ordered_value(f.gkey[g]);
+    if (f.gnz[g] && n > 1 && mx != -INFINITY && 32 * (i >> 5) < n) {
+      const bool valid = i < n;
+      const double e = valid ? scaled_weight(f, base + i, mx) : 0.0;
+      const double incl = warp_inclusive_scan(e);
+      if (valid) {
+        f.ew[base + i] = e;
+        f.pre[base + i] = incl;
+      }
+      if ((i & 31) == 31) {
+        f.chunk_sum[f.chunk_first[g] + (i >> 5)] = incl;
+      }
+    }
+    cluster.sync();  // 1: chunk totals and the zeroed flag are in place
+    if (rank == 0 && threadIdx.x < 32) {
+      group_update(f, g, threadIdx.x);
+    }
+    cluster.sync();  // 2: mode, offsets and the target spacing
+    const int mode = f.mode[g];
+    int* flag0 = cluster.map_shared_rank(&flag, 0);
+    if (i < n) {
+      if (mode == MODE_FIRST) {
+        f.idx[base + i] = 0;
+      } else if (mode == MODE_RESAMPLE) {
+        resample_particle(f, g, i, base + i, flag0);
+      }
+    }
+    cluster.sync();  // 3: every decision and its flag
+    const bool serial = mode == MODE_RESAMPLE &&
+      (*flag0 != 0 || *f.force_serial != 0);
+    if (serial && rank == 0) {
+      serial_fallback(f, g, count);
+    }
+    cluster.sync();  // 4: the serial indices; rank 0's flag is done with
+  }
+  if (i < n) {
+    const int k = base + i;
+    const int from = f.mode[g] != MODE_KEEP ? base + f.idx[k] : k;
+    for (int s = 0; s < n_state; ++s) {
+      dst[static_cast<long>(s) * stride + k] =
+        src[static_cast<long>(s) * stride + from];
+    }
   }
 }
 

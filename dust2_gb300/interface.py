@@ -753,10 +753,20 @@ class DustLikelihood:
         self.deterministic = False
         self._handle = None
         self.n_state = None
+        # run options, applied to the engine object when it is created
+        self.serial_resample = False
+        self.fused_tail = True
 
     @property
     def ptr(self):
         return self._handle
+
+    def apply_options(self):
+        lib = _lib.lib()
+        check(lib.dust2_gb300_filter_set_serial_resample(
+            self._handle, 1 if self.serial_resample else 0))
+        check(lib.dust2_gb300_filter_set_fused_tail(
+            self._handle, 1 if self.fused_tail else 0))
 
     def initialise(self, pars):
         flat = as_f64(np.concatenate([self.generator.pack_pars(p)
@@ -795,6 +805,7 @@ class DustLikelihood:
                 uptr(words), words.size, ctypes.byref(handle)))
         self._handle = handle
         self.initial_rng_state = None
+        self.apply_options()
         n_state = ctypes.c_size_t()
         n_tot = ctypes.c_size_t()
         n_g = ctypes.c_size_t()
@@ -1289,11 +1300,29 @@ def scale_log_weights(w):
     return r.value, w
 
 
+def _check_filter(obj):
+    if not isinstance(obj, DustLikelihood):
+        raise DustError("Expected 'obj' to be a particle filter")
+
+
 def dust_likelihood_set_serial_resample(obj, serial):
-    """Verification mode: resample every group with the serial algorithm."""
-    _check_lik(obj)
-    check(_lib.lib().dust2_gb300_filter_set_serial_resample(
-        obj.ptr, 1 if serial else 0))
+    """Verification mode: resample every group with the serial algorithm.
+    Kept by the object, so it may be set before the first run."""
+    _check_filter(obj)
+    obj.serial_resample = bool(serial)
+    if obj.ptr is not None:
+        obj.apply_options()
+
+
+def dust_likelihood_set_fused_tail(obj, fused):
+    """Tuning switch: run each observation's weights, resampling and
+    reorder as one launch when every group has at most 1024 particles
+    (the default), or as separate kernels.  The results are identical.
+    Kept by the object, so it may be set before the first run."""
+    _check_filter(obj)
+    obj.fused_tail = bool(fused)
+    if obj.ptr is not None:
+        obj.apply_options()
 
 
 def dust_likelihood_serial_fallbacks(obj):

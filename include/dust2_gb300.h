@@ -368,6 +368,14 @@ int dust2_gb300_resample_weight_noalloc(const double* w, size_t n, double u,
 int dust2_gb300_filter_set_serial_resample(dust2_gb300_filter* filter,
                                            int32_t serial);
 
+/* 1 (default): when every group has at most 1024 particles, the weights,
+ * log-likelihood, resampling and reorder of an observation run as one
+ * launch with one block per group; 0: as separate kernels over the whole
+ * particle range.  The results are identical; this is a tuning switch
+ * with no counterpart in dust2. */
+int dust2_gb300_filter_set_fused_tail(dust2_gb300_filter* filter,
+                                      int32_t fused);
+
 /* Asynchronous form of dust2_gb300_filter_run (system initial conditions,
  * current parameters): enqueues the run on the filter's CUDA stream and
  * returns; results stay on the device.  No counterpart in dust2, whose

@@ -153,6 +153,15 @@ def test_filter_create_validation_without_device(built):
         d.dust_likelihood_run(obj, None)
     with pytest.raises(d.DustError, match="'index_group' must be NULL"):
         d.dust_likelihood_run(obj, {"beta": 0.1}, index_group=[1])
+    # run options set before the first run are kept for the engine object
+    from dust2_gb300 import interface
+    assert obj.fused_tail and not obj.serial_resample
+    interface.dust_likelihood_set_fused_tail(obj, False)
+    interface.dust_likelihood_set_serial_resample(obj, True)
+    assert not obj.fused_tail and obj.serial_resample
+    unf = d.dust_unfilter_create(d.sir(), 0, data)
+    with pytest.raises(d.DustError, match="Expected 'obj' to be a particle"):
+        interface.dust_likelihood_set_fused_tail(unf, True)
 
 
 def test_invalid_handles_are_errors(built):
@@ -161,6 +170,8 @@ def test_invalid_handles_are_errors(built):
     assert lib.dust2_gb300_system_time(None, ctypes.byref(t)) == 1
     assert "Invalid system handle" in _lib.last_error()
     assert lib.dust2_gb300_filter_run(None, None, None, 0, None) == 1
+    assert "Invalid filter handle" in _lib.last_error()
+    assert lib.dust2_gb300_filter_set_fused_tail(None, 1) == 1
     assert "Invalid filter handle" in _lib.last_error()
 
 

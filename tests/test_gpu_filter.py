@@ -326,6 +326,47 @@ def test_forced_serial_resampling_is_identical(port):
     assert_ll(res[0][0], res[1][0])
 
 
+@pytest.mark.parametrize("n_particles", [[1000, 1, 33, 512, 1024, 96],
+                                         [700, 700, 700]])
+def test_fused_tail_is_identical(n_particles):
+    """The one-launch tail for groups of at most 1024 particles and the
+    separate kernels give the same bits: log-likelihoods (including a group
+    whose weights are all -Inf, and a one-particle group), final states,
+    generator states and (equal groups) trajectories, with and without
+    forced serial resampling."""
+    from dust2_gb300 import interface
+    gen = d.sir_cases()
+    plist, times, data = _uneven_case(8, n_particles, n_times=25)
+    G = len(n_particles)
+    data[:, G - 1] = 1e307  # every particle's log density is -Inf
+    traj = len(set(n_particles)) == 1
+    cols = {"time": np.repeat(times, G), "group": np.tile(np.arange(1, G + 1),
+                                                          times.size),
+            "incidence": data.ravel()}
+    for serial in (False, True):
+        res = []
+        for fused in (True, False):
+            obj = d.dust_filter_create(gen, 0, cols, n_particles=n_particles,
+                                       dt=0.25, seed=11)
+            interface.dust_likelihood_set_fused_tail(obj, fused)
+            interface.dust_likelihood_set_serial_resample(obj, serial)
+            ll = [d.dust_likelihood_run(obj, plist, save_trajectories=traj)
+                  for _ in range(2)]
+            res.append((np.array(ll),
+                        d.dust_likelihood_last_trajectories(obj) if traj
+                        else None,
+                        d.dust_likelihood_last_state(obj),
+                        d.dust_likelihood_rng_state(obj),
+                        d.dust_likelihood_serial_fallbacks(obj)))
+        assert np.all(np.isneginf(res[0][0][:, G - 1]))
+        assert np.all(np.isfinite(res[0][0][:, :G - 1]))
+        np.testing.assert_array_equal(res[0][0], res[1][0])
+        np.testing.assert_array_equal(res[0][1], res[1][1])
+        np.testing.assert_array_equal(res[0][2], res[1][2])
+        assert res[0][3] == res[1][3]
+        assert res[0][4] == res[1][4]
+
+
 def test_resample_weight_hook(port):
     """test-filter-details.R:1-22 through the GPU kernels, including exact
     ties, where the parallel decision must defer to the serial one."""
