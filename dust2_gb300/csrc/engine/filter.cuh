@@ -12,7 +12,8 @@
 //   2. k_weights       w = exp(logw - max); one warp per 32-particle
 //                      chunk of a group: inclusive prefix sums and the
 //                      chunk total (FP64).
-//   3. k_group         one warp per group: scan of the chunk totals, the
+//   3. k_group         one block per group: scan of the chunk totals
+//                      (one warp per window of 32 chunks), the
 //                      log-likelihood increment log(sum/n) + max (:32-38),
 //                      and the uniform u from the group's filter stream 2g
 //                      (filter.hpp:75).
@@ -38,6 +39,10 @@
 // (step 5), which is the reference algorithm verbatim.  The
 // log-likelihood uses the parallel total; it matches the serial one to
 // better than n u relative (u = 2^-53).
+//
+// When every group has at most 1024 particles, steps 2-6 run as one
+// launch, k_tail_cluster (a cluster of blocks per group), with the same
+// results.
 //
 // The whole sequence for all data times is captured once into a CUDA
 // graph and replayed on every run.
@@ -384,6 +389,12 @@ public:
     put_rng_state(rng_words.data());
     sys_->sync();
     set_fused_tail(true);
+    // k_group: one warp per window of 32 chunks of the largest group
+    int n_win = 1;
+    for (int c : L.chunk_count) {
+      n_win = std::max(n_win, (c + 31) / 32);
+    }
+    group_threads_ = 32 * std::min(n_win, 32);
   }
 
   system_api& sys() override {
@@ -885,7 +896,7 @@ private:
           f, fallback_count_.data(), cur, other, L.stride, S.n_state());
       } else {
         k_weights<<<NT, TS, 0, s>>>(f);
-        k_group<<<G, 32, 0, s>>>(f, G);
+        k_group<<<G, group_threads_, 0, s>>>(f, G);
         k_resample<<<NT, TS, 0, s>>>(f);
         k_fallback_counted(f, s);
         k_reorder<<<NT, TS, 0, s>>>(cur, other, L.stride, S.n_state(),
@@ -1010,6 +1021,7 @@ private:
   bool has_run_ = false;
   bool use_graph_ = true;
   bool fused_tail_ = false;  // k_tail_cluster instead of separate kernels
+  int group_threads_ = 32;   // block size of k_group
   bool pending_ = false;
   bool capturing_ = false;
   bool timing_ = false;

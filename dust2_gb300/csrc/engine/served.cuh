@@ -992,7 +992,7 @@ private:
       DUST2_CUDA(cudaEventRecord(r.step1, s));
     }
     k_weights<<<NT, TS, 0, s>>>(f);
-    k_group<<<S, 32, 0, s>>>(f, S);
+    k_group<<<S, 256, 0, s>>>(f, S);
     k_resample<<<NT, TS, 0, s>>>(f);
     k_fallback_count<<<S, 256, 0, s>>>(f, fallback_count_.data());
     k_reorder_active<<<NT, TS, 0, s>>>(cur(), other(), cap_particles_,

@@ -68,58 +68,124 @@ __global__ void k_weights(filter_view f) {
   }
 }
 
-// One warp of a running group: chunk offsets, log-likelihood increment
-// and the resampling uniform; then clear the per-observation reductions.
-__device__ void group_update(const filter_view& f, int g, int lane) {
+// Whether a group's weights are summed at this observation: some weight
+// is not 0, more than one particle, and not every log weight -Inf.
+__device__ __forceinline__ bool group_has_sum(const filter_view& f, int g) {
+  return f.gnz[g] != 0 && f.n_particles[g] > 1 &&
+    ordered_value(f.gkey[g]) != -INFINITY;
+}
+
+// One thread, given the group's weight total: log-likelihood increment,
+// mode and resampling uniform; then clear the per-observation reductions.
+__device__ void group_finish(const filter_view& f, int g, double tot) {
   const int n = f.n_particles[g];
   const bool nz = f.gnz[g] != 0;
   const double mx = ordered_value(f.gkey[g]);
   int mode = MODE_KEEP;
-  double tot = 0;
-  if (nz && n > 1 && mx != -INFINITY) {
-    tot = group_chunk_offsets(f, g, lane);
-  }
-  if (lane == 0) {
-    if (nz) {
-      random::rng_state r{};
-      for (int w = 0; w < 4; ++w) {
-        r.state[w] = f.frng[8 * g + w];
-      }
-      r.deterministic = false;
-      double inc;
-      if (n == 1) {
-        inc = f.w[f.offset[g]];
-        mode = MODE_FIRST;
-      } else if (mx == -INFINITY) {
-        inc = -INFINITY;
-        mode = MODE_FIRST;
-      } else {
-        inc = math::log(tot / n) + mx;
-        mode = MODE_RESAMPLE;
-      }
-      f.ll[g] += inc;
-      const double u = random::random_real(r);
-      for (int w = 0; w < 4; ++w) {
-        f.frng[8 * g + w] = r.state[w];
-      }
-      f.gu[g] = u;
-      f.gtot[g] = tot;
-      f.guu0[g] = tot * u / n;
-      f.gdu[g] = tot / n;
+  if (nz) {
+    random::rng_state r{};
+    for (int w = 0; w < 4; ++w) {
+      r.state[w] = f.frng[8 * g + w];
     }
-    f.mode[g] = mode;
-    f.gkey[g] = ordered_key(-INFINITY);
-    f.gnz[g] = 0;
-    f.gflag[g] = (mode == MODE_RESAMPLE && *f.force_serial) ? 1 : 0;
+    r.deterministic = false;
+    double inc;
+    if (n == 1) {
+      inc = f.w[f.offset[g]];
+      mode = MODE_FIRST;
+    } else if (mx == -INFINITY) {
+      inc = -INFINITY;
+      mode = MODE_FIRST;
+    } else {
+      inc = math::log(tot / n) + mx;
+      mode = MODE_RESAMPLE;
+    }
+    f.ll[g] += inc;
+    const double u = random::random_real(r);
+    for (int w = 0; w < 4; ++w) {
+      f.frng[8 * g + w] = r.state[w];
+    }
+    f.gu[g] = u;
+    f.gtot[g] = tot;
+    f.guu0[g] = tot * u / n;
+    f.gdu[g] = tot / n;
+  }
+  f.mode[g] = mode;
+  f.gkey[g] = ordered_key(-INFINITY);
+  f.gnz[g] = 0;
+  f.gflag[g] = (mode == MODE_RESAMPLE && *f.force_serial) ? 1 : 0;
+}
+
+// One warp of a running group: chunk offsets, then group_finish.
+__device__ void group_update(const filter_view& f, int g, int lane) {
+  const double tot = group_has_sum(f, g) ?
+    group_chunk_offsets(f, g, lane) : 0.0;
+  if (lane == 0) {
+    group_finish(f, g, tot);
   }
 }
 
+// group_chunk_offsets with the whole block: warp w scans windows w,
+// w + (warps), ... of 32 chunks at once, thread 0 accumulates the window
+// totals in window order (the running carry of the one-warp loop), and
+// each warp adds its window's carry.  Every sum is the one the one-warp
+// loop forms, so the results are the same bits; a group of 32,768
+// particles takes one pass instead of 32 dependent ones.  The total is
+// returned to thread 0.
+__device__ double group_chunk_offsets_block(const filter_view& f, int g) {
+  __shared__ double win_total[32];
+  __shared__ double win_carry[32];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int n_warps = blockDim.x >> 5;
+  const int c0 = f.chunk_first[g];
+  const int nc = f.chunk_count[g];
+  const int n_win = (nc + 31) >> 5;
+  double carry = 0;  // thread 0
+  for (int wb = 0; wb < n_win; wb += n_warps) {
+    const int w = wb + warp;
+    const int c = 32 * w + lane;
+    double v = 0, excl = 0;
+    if (w < n_win) {
+      v = c < nc ? f.chunk_sum[c0 + c] : 0.0;
+      const double incl = warp_inclusive_scan(v);
+      excl = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (lane == 0) {
+        excl = 0;
+      }
+      if (lane == 31) {
+        win_total[warp] = incl;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int m = min(n_warps, n_win - wb);
+      for (int j = 0; j < m; ++j) {
+        win_carry[j] = carry;
+        carry = carry + win_total[j];
+      }
+    }
+    __syncthreads();
+    if (w < n_win && c < nc) {
+      const double off = win_carry[warp] + excl;
+      f.chunk_off[c0 + c] = off;
+      f.chunk_sum[c0 + c] = off + v;
+    }
+  }
+  return carry;
+}
+
+// One block (a multiple of 32 threads, at most 1024) per group.
 __global__ void k_group(filter_view f, int n_groups) {
   const int g = blockIdx.x;
   if (g >= n_groups || !f.active[g]) {
     return;
   }
-  group_update(f, g, threadIdx.x);
+  const double tot = group_has_sum(f, g) ?
+    group_chunk_offsets_block(f, g) : 0.0;
+  __syncthreads();  // every thread has read the reductions group_finish clears
+  if (threadIdx.x == 0) {
+    group_finish(f, g, tot);
+  }
 }
 
 // Prefix sum Q_m (weights 0..m of the group) for group-local index m.
