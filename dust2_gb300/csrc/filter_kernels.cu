@@ -75,19 +75,35 @@ __device__ __forceinline__ bool group_has_sum(const filter_view& f, int g) {
     ordered_value(f.gkey[g]) != -INFINITY;
 }
 
-// One thread, given the group's weight total: log-likelihood increment,
-// mode and resampling uniform; then clear the per-observation reductions.
-__device__ void group_finish(const filter_view& f, int g, double tot) {
+// The next draw of a group's filter stream (filter.hpp:75), taken before
+// it is known to be needed; group_finish keeps it, and the advanced
+// stream, only for a group with data.
+struct group_uniform {
+  random::rng_state r;
+  double u;
+};
+
+__device__ group_uniform draw_group_uniform(const filter_view& f, int g) {
+  group_uniform d{};
+  for (int w = 0; w < 4; ++w) {
+    d.r.state[w] = f.frng[8 * g + w];
+  }
+  d.r.deterministic = false;
+  d.u = random::random_real(d.r);
+  return d;
+}
+
+// One thread, given the group's weight total and the draw: log-likelihood
+// increment, mode and resampling uniform; then clear the per-observation
+// reductions.
+__device__ void group_finish(const filter_view& f, int g, double tot,
+                             const group_uniform& d) {
   const int n = f.n_particles[g];
   const bool nz = f.gnz[g] != 0;
   const double mx = ordered_value(f.gkey[g]);
   int mode = MODE_KEEP;
   if (nz) {
-    random::rng_state r{};
-    for (int w = 0; w < 4; ++w) {
-      r.state[w] = f.frng[8 * g + w];
-    }
-    r.deterministic = false;
+    const double mean = tot / n;
     double inc;
     if (n == 1) {
       inc = f.w[f.offset[g]];
@@ -96,18 +112,17 @@ __device__ void group_finish(const filter_view& f, int g, double tot) {
       inc = -INFINITY;
       mode = MODE_FIRST;
     } else {
-      inc = math::log(tot / n) + mx;
+      inc = math::log(mean) + mx;
       mode = MODE_RESAMPLE;
     }
     f.ll[g] += inc;
-    const double u = random::random_real(r);
     for (int w = 0; w < 4; ++w) {
-      f.frng[8 * g + w] = r.state[w];
+      f.frng[8 * g + w] = d.r.state[w];
     }
-    f.gu[g] = u;
+    f.gu[g] = d.u;
     f.gtot[g] = tot;
-    f.guu0[g] = tot * u / n;
-    f.gdu[g] = tot / n;
+    f.guu0[g] = tot * d.u / n;
+    f.gdu[g] = mean;
   }
   f.mode[g] = mode;
   f.gkey[g] = ordered_key(-INFINITY);
@@ -120,7 +135,7 @@ __device__ void group_update(const filter_view& f, int g, int lane) {
   const double tot = group_has_sum(f, g) ?
     group_chunk_offsets(f, g, lane) : 0.0;
   if (lane == 0) {
-    group_finish(f, g, tot);
+    group_finish(f, g, tot, draw_group_uniform(f, g));
   }
 }
 
@@ -184,31 +199,49 @@ __global__ void k_group(filter_view f, int n_groups) {
     group_chunk_offsets_block(f, g) : 0.0;
   __syncthreads();  // every thread has read the reductions group_finish clears
   if (threadIdx.x == 0) {
-    group_finish(f, g, tot);
+    group_finish(f, g, tot, draw_group_uniform(f, g));
   }
 }
 
-// Prefix sum Q_m (weights 0..m of the group) for group-local index m.
-__device__ __forceinline__ double prefix_at(const filter_view& f, int g,
-                                            int m) {
-  return f.chunk_off[f.chunk_first[g] + (m >> 5)] + f.pre[f.offset[g] + m];
+// What the resampling search of one group reads: its chunk ends and
+// offsets (left by k_group), its chunk-local prefix sums and the targets'
+// start and spacing.  The arrays may be the global ones or copies.
+struct search_view {
+  const double* chunk_end;  // [nc]
+  const double* chunk_off;  // [nc]
+  const double* pre;        // [n]
+  int n;
+  int nc;
+  double uu0;
+  double du;
+};
+
+__device__ __forceinline__ search_view group_search(const filter_view& f,
+                                                    int g) {
+  const int c0 = f.chunk_first[g];
+  return search_view{f.chunk_sum + c0, f.chunk_off + c0,
+                     f.pre + f.offset[g], f.n_particles[g],
+                     f.chunk_count[g], f.guu0[g], f.gdu[g]};
 }
 
-// The resampling index of particle i (global index k) of a group being
-// resampled; an ambiguous decision is recorded in *flag.
-__device__ void resample_particle(const filter_view& f, int g, int i, int k,
-                                  int* flag) {
-  const int n = f.n_particles[g];
-  const double uu = f.guu0[g] + static_cast<double>(i) * f.gdu[g];
+// Prefix sum Q_m (weights 0..m of the group) for group-local index m.
+__device__ __forceinline__ double prefix_at(const search_view& sv, int m) {
+  return sv.chunk_off[m >> 5] + sv.pre[m];
+}
+
+// The resampling index of particle i of a group being resampled; an
+// ambiguous decision is recorded in *flag.
+__device__ int resample_index(const search_view& sv, int i, int* flag) {
+  const int n = sv.n;
+  const double uu = sv.uu0 + static_cast<double>(i) * sv.du;
   // first chunk whose last prefix (its end, left in chunk_sum by k_group)
   // reaches uu; every value compared is >= +0, so the comparisons are
   // taken on the bits
-  const int c0 = f.chunk_first[g];
-  const int nc = f.chunk_count[g];
+  const int nc = sv.nc;
   int lo = 0, hi = nc;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
-    if (math::le_nonneg(uu, f.chunk_sum[c0 + mid])) {
+    if (math::le_nonneg(uu, sv.chunk_end[mid])) {
       hi = mid;
     } else {
       lo = mid + 1;
@@ -221,8 +254,8 @@ __device__ void resample_particle(const filter_view& f, int g, int i, int k,
     const int first = lo * 32;
     const int last = min(n, first + 32) - 1;
     int a = first, b = last;
-    const double off = f.chunk_off[c0 + lo];
-    const double* pre = f.pre + f.offset[g];
+    const double off = sv.chunk_off[lo];
+    const double* pre = sv.pre;
     while (a < b) {
       const int mid = (a + b) >> 1;
       if (math::le_nonneg(uu, off + pre[mid])) {
@@ -254,19 +287,19 @@ __device__ void resample_particle(const filter_view& f, int g, int i, int k,
   const double eps = 0x1.0p-53 * 1.05;
   bool ok = true;
   if (m > 0) {
-    const double p = prefix_at(f, g, m - 1);
+    const double p = prefix_at(sv, m - 1);
     const double margin = eps * (m + n + 2 * L + 16) * fmax(p, uu);
     ok = ok && p < uu - margin;
   }
   if (m < n - 1) {
-    const double q = prefix_at(f, g, m);
+    const double q = prefix_at(sv, m);
     const double margin = eps * (m + 1 + n + 2 * L + 16) * fmax(q, uu);
     ok = ok && q >= uu + margin;
   }
-  f.idx[k] = m;
   if (!ok) {
     atomicOr(flag, 1);
   }
+  return m;
 }
 
 __global__ void k_resample(filter_view f) {
@@ -284,7 +317,8 @@ __global__ void k_resample(filter_view f) {
     f.idx[k] = 0;
     return;
   }
-  resample_particle(f, g, tl.local + threadIdx.x, k, f.gflag + g);
+  f.idx[k] = resample_index(group_search(f, g), tl.local + threadIdx.x,
+                            f.gflag + g);
 }
 
 // The reference algorithm (filter_details.hpp:45-74) for groups with an
@@ -367,35 +401,50 @@ __global__ void k_fallback_count(filter_view f, int* count) {
 // separated by cluster barriers, whose release/acquire semantics make the
 // global writes of one phase visible to the next.  Every value is
 // computed by the same device functions in the same order as by the
-// separate kernels, so the results are the same bits.  Every block of a
-// running group takes all four barriers whatever the data, so no barrier
-// can wait for a block that has left.  The state of every group moves
-// from src to dst (in place for groups that keep their particles), as
-// k_reorder does.
+// separate kernels, so the results are the same bits.  To shorten the
+// chain of dependent loads, the group's filter draw is taken before the
+// weights are summed, and each block searches shared-memory copies of the
+// group's prefix sums.  Every block of a running group takes all four
+// barriers whatever the data (the fourth as arrive and wait around the
+// state copy when no serial fallback runs; that choice is the same in
+// every block), so no barrier can wait for a block that has left.  The
+// state of every group moves from src to dst (in place for groups that
+// keep their particles), as k_reorder does.
 __global__ void __cluster_dims__(TAIL_CLUSTER, 1, 1)
 __launch_bounds__(TAIL_BLOCK)
 k_tail_cluster(filter_view f, int* count, const double* __restrict__ src,
                double* __restrict__ dst, int stride, int n_state) {
   __shared__ int flag;  // ambiguous decisions, used in block rank 0
+  // copies of the group's search arrays (n <= TAIL_MAX_PARTICLES)
+  __shared__ double s_end[TAIL_MAX_PARTICLES / 32];
+  __shared__ double s_off[TAIL_MAX_PARTICLES / 32];
+  __shared__ double s_pre[TAIL_MAX_PARTICLES];
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int g = blockIdx.x / TAIL_CLUSTER;
   const int rank = static_cast<int>(cluster.block_rank());
   const int i = rank * TAIL_BLOCK + static_cast<int>(threadIdx.x);
+  const bool active = f.active[g] != 0;
   const int n = f.n_particles[g];
   const int base = f.offset[g];
-  if (f.active[g]) {
-    if (threadIdx.x == 0) {
+  const int k = base + i;
+  int from = k;  // the source of this particle's state
+  bool arrived = false;  // barrier 4 arrived on, still to be waited for
+  if (active) {
+    const bool summed = group_has_sum(f, g);
+    group_uniform draw{};
+    if (rank == 0 && threadIdx.x == 0) {
       flag = 0;
+      draw = draw_group_uniform(f, g);  // independent of the weights
     }
-    const double mx = ordered_value(f.gkey[g]);
-    if (f.gnz[g] && n > 1 && mx != -INFINITY && 32 * (i >> 5) < n) {
+    if (summed && 32 * (i >> 5) < n) {
       const bool valid = i < n;
-      const double e = valid ? scaled_weight(f, base + i, mx) : 0.0;
+      const double e =
+        valid ? scaled_weight(f, k, ordered_value(f.gkey[g])) : 0.0;
       const double incl = warp_inclusive_scan(e);
       if (valid) {
-        f.ew[base + i] = e;
-        f.pre[base + i] = incl;
+        f.ew[k] = e;
+        f.pre[k] = incl;
       }
       if ((i & 31) == 31) {
         f.chunk_sum[f.chunk_first[g] + (i >> 5)] = incl;
@@ -403,33 +452,66 @@ k_tail_cluster(filter_view f, int* count, const double* __restrict__ src,
     }
     cluster.sync();  // 1: chunk totals and the zeroed flag are in place
     if (rank == 0 && threadIdx.x < 32) {
-      group_update(f, g, threadIdx.x);
+      const double tot =
+        summed ? group_chunk_offsets(f, g, threadIdx.x) : 0.0;
+      if (threadIdx.x == 0) {
+        group_finish(f, g, tot, draw);
+      }
     }
     cluster.sync();  // 2: mode, offsets and the target spacing
     const int mode = f.mode[g];
+    const double uu0 = f.guu0[g];
+    const double du = f.gdu[g];
+    const int c0 = f.chunk_first[g];
+    const int nc = f.chunk_count[g];
     int* flag0 = cluster.map_shared_rank(&flag, 0);
-    if (i < n) {
-      if (mode == MODE_FIRST) {
-        f.idx[base + i] = 0;
-      } else if (mode == MODE_RESAMPLE) {
-        resample_particle(f, g, i, base + i, flag0);
+    if (mode == MODE_RESAMPLE) {
+      for (int j = threadIdx.x; j < nc; j += TAIL_BLOCK) {
+        s_end[j] = f.chunk_sum[c0 + j];
+        s_off[j] = f.chunk_off[c0 + j];
       }
+      for (int j = threadIdx.x; j < n; j += TAIL_BLOCK) {
+        s_pre[j] = f.pre[base + j];
+      }
+      __syncthreads();
+      if (i < n) {
+        const search_view sv{s_end, s_off, s_pre, n, nc, uu0, du};
+        const int m = resample_index(sv, i, flag0);
+        f.idx[k] = m;
+        from = base + m;
+      }
+    } else if (mode == MODE_FIRST && i < n) {
+      f.idx[k] = 0;
+      from = base;
     }
     cluster.sync();  // 3: every decision and its flag
+    // the same for every block: rank 0's flag is final and no longer
+    // written, the force flag is read-only
     const bool serial = mode == MODE_RESAMPLE &&
       (*flag0 != 0 || *f.force_serial != 0);
-    if (serial && rank == 0) {
-      serial_fallback(f, g, count);
+    if (serial) {
+      if (rank == 0) {
+        serial_fallback(f, g, count);
+      }
+      cluster.sync();  // 4: the serial indices are in place
+      if (i < n) {
+        from = base + f.idx[k];
+      }
+    } else {
+      // 4, split: rank 0's shared memory must outlive every block's read
+      // of its flag, but the copy below need not wait
+      cluster.barrier_arrive();
+      arrived = true;
     }
-    cluster.sync();  // 4: the serial indices; rank 0's flag is done with
   }
   if (i < n) {
-    const int k = base + i;
-    const int from = f.mode[g] != MODE_KEEP ? base + f.idx[k] : k;
     for (int s = 0; s < n_state; ++s) {
       dst[static_cast<long>(s) * stride + k] =
         src[static_cast<long>(s) * stride + from];
     }
+  }
+  if (arrived) {
+    cluster.barrier_wait();
   }
 }
 
