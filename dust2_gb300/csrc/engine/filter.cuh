@@ -279,6 +279,8 @@ __device__ __forceinline__ double group_chunk_offsets(const filter_view& f,
 __global__ void k_weights(filter_view f);
 __global__ void k_group(filter_view f, int n_groups);
 __global__ void k_resample(filter_view f);
+// Block size of k_fallback_count (any multiple of 32 up to 1024 works).
+constexpr int FALLBACK_THREADS = 1024;
 // The one-launch tail: a cluster of TAIL_CLUSTER blocks of TAIL_BLOCK
 // threads per group, for groups of at most TAIL_MAX_PARTICLES.
 constexpr int TAIL_CLUSTER = 8;
@@ -1070,7 +1072,7 @@ __global__ void k_fallback_count(filter_view f, int* count);
 template <typename T>
 void filter_engine<T>::k_fallback_counted(filter_view f, cudaStream_t s) {
   const int G = sys_->layout().n_groups;
-  k_fallback_count<<<G, 256, 0, s>>>(f, fallback_count_.data());
+  k_fallback_count<<<G, FALLBACK_THREADS, 0, s>>>(f, fallback_count_.data());
 }
 
 }  // namespace engine

@@ -994,7 +994,8 @@ private:
     k_weights<<<NT, TS, 0, s>>>(f);
     k_group<<<S, 256, 0, s>>>(f, S);
     k_resample<<<NT, TS, 0, s>>>(f);
-    k_fallback_count<<<S, 256, 0, s>>>(f, fallback_count_.data());
+    k_fallback_count<<<S, FALLBACK_THREADS, 0, s>>>(f,
+                                                    fallback_count_.data());
     k_reorder_active<<<NT, TS, 0, s>>>(cur(), other(), cap_particles_,
                                        n_state_, tiles_.data(),
                                        active_.data(), offset_.data(),

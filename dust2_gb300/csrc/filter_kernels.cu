@@ -322,43 +322,207 @@ __global__ void k_resample(filter_view f) {
 }
 
 // The reference algorithm (filter_details.hpp:45-74) for groups with an
-// ambiguous parallel decision.  Its serial running sum ww_j =
-// fl(ww_{j-1} + w_j) is computed exactly as the reference does, by one
-// thread, with the weights staged through shared memory in chunks; the
-// reference's walk over particles then equals, for each particle, the
-// first j with ww_j >= uu_i (ww is non-decreasing because the weights are
-// non-negative and rounding is monotone), which the whole block finds by
-// binary search.  The serial sums overwrite this group's `pre` entries.
-constexpr int FALLBACK_CHUNK = 2048;
+// ambiguous parallel decision.  Its running sum ww_j = fl(ww_{j-1} + w_j)
+// is reproduced exactly (exact_running_sums); the reference's walk over
+// particles then equals, for each particle, the first j with ww_j >= uu_i
+// (ww is non-decreasing because the weights are non-negative and
+// rounding is monotone), which the whole block finds by binary search.
+// The running sums overwrite this group's `pre` entries.
+//
+// Exact running sums in parallel.  While the running sum stays within one
+// binade [2^e, 2^(e+1)), every sum it takes is rounded to the same grid
+// of multiples of ulp = 2^(e-52), so fl(s + w) = s + ulp * r with
+// r = round(w / ulp) an integer that does not depend on s (the one
+// exception is a tie, w / ulp exactly halfway between integers, which
+// rounds to the even sum).  Within a binade the running sum is therefore
+// a prefix sum of integers, which is associative: the block scans the
+// integers r of a window of weights, and every position before the first
+// one that would leave the binade (or is a tie) gets its exact value.
+// That one step is taken with a real FP64 add, and the next window starts
+// after it.  A run of weights whose breaks come within 32 positions of
+// each other (the first steps, when the sum is small) is added one by one
+// by thread 0, which bounds the cost by about that of the plain loop.
+// A sum that is Inf, NaN or negative (weights outside the contract)
+// continues one by one.  The steps taken are the
+// reference's own, so the sums are the same bits; a group of 32,768
+// particles takes ~50 block-wide windows instead of 32,768 dependent
+// FP64 adds.
+
+__device__ __forceinline__ unsigned long long sat_add(unsigned long long a,
+                                                      unsigned long long b) {
+  const unsigned long long c = a + b;  // both <= 2^62: no wrap
+  return c > (1ull << 62) ? (1ull << 62) : c;
+}
+
+// round(w / 2^e_s) for w >= 0 as an integer, saturated at 2^62; *tie when
+// w / 2^e_s is exactly halfway between two integers.
+__device__ __forceinline__ unsigned long long grid_units(double w, int e_s,
+                                                         bool* tie) {
+  const unsigned long long wb = __double_as_longlong(w);
+  const int be = static_cast<int>(wb >> 52);
+  unsigned long long m = wb & ((1ull << 52) - 1);
+  int e_w = -1074;
+  if (be != 0) {
+    m |= 1ull << 52;
+    e_w = be - 1075;
+  }
+  *tie = false;
+  if (m == 0) {
+    return 0;
+  }
+  const int d = e_w - e_s;
+  if (d >= 0) {
+    if (d >= 62 || (m >> (62 - d)) != 0) {
+      return 1ull << 62;
+    }
+    return m << d;
+  }
+  const int sh = -d;
+  if (sh > 54) {
+    return 0;  // below half a unit (m < 2^53)
+  }
+  unsigned long long q = m >> sh;
+  const unsigned long long rem = m & ((1ull << sh) - 1);
+  const unsigned long long half = 1ull << (sh - 1);
+  if (rem > half) {
+    q += 1;
+  } else if (rem == half) {
+    *tie = true;
+  }
+  return q;
+}
+
+// Inclusive block scan of saturating sums (blockDim.x a multiple of 32,
+// at most 1024).  Ends with the block synchronised.
+__device__ unsigned long long block_scan_sat(unsigned long long v,
+                                             unsigned long long* warp_tot) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int n_warps = blockDim.x >> 5;
+  for (int off = 1; off < 32; off <<= 1) {
+    const unsigned long long t = __shfl_up_sync(0xffffffffu, v, off);
+    if (lane >= off) {
+      v = sat_add(v, t);
+    }
+  }
+  if (lane == 31) {
+    warp_tot[warp] = v;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long x = lane < n_warps ? warp_tot[lane] : 0;
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) {
+        x = sat_add(x, t);
+      }
+    }
+    if (lane < n_warps) {
+      warp_tot[lane] = x;
+    }
+  }
+  __syncthreads();
+  if (warp > 0) {
+    v = sat_add(v, warp_tot[warp - 1]);
+  }
+  __syncthreads();  // warp_tot may be rewritten by the next call
+  return v;
+}
+
+// ser[j] = fl(ser[j-1] + w[j]), ser[0] = w[0], for n >= 1 non-negative
+// weights, by the whole block; returns ser[n-1] to every thread.
+__device__ double exact_running_sums(const double* w, double* ser, int n) {
+  __shared__ unsigned long long warp_tot[32];
+  __shared__ int first_break;
+  __shared__ int s_j0;
+  __shared__ double s_sum;
+  const int nb = static_cast<int>(blockDim.x);
+  const int t = threadIdx.x;
+  if (t == 0) {
+    s_j0 = 0;
+    s_sum = w[0];  // fl(0 + w_0)
+    ser[0] = w[0];
+  }
+  __syncthreads();
+  for (;;) {
+    const int j0 = s_j0;
+    const double sum = s_sum;
+    if (j0 >= n - 1) {
+      break;
+    }
+    const unsigned long long sb = __double_as_longlong(sum);
+    const int be = static_cast<int>(sb >> 52);
+    if (be >= 2047) {  // Inf, NaN or negative: the rest one by one
+      if (t == 0) {
+        double acc = sum;
+        for (int j = j0 + 1; j < n; ++j) {
+          acc = acc + w[j];
+          ser[j] = acc;
+        }
+        s_sum = acc;
+      }
+      __syncthreads();
+      break;
+    }
+    // sum = (base + m_sum) as bits, with the grid 2^e_s of its binade
+    // (subnormals share the grid of the first normal binade)
+    const int bep = be < 1 ? 1 : be;
+    const int e_s = bep - 1075;
+    const unsigned long long base = static_cast<unsigned long long>(bep - 1)
+      << 52;
+    const unsigned long long m_sum = sb - base;
+    const int j = j0 + 1 + t;
+    bool tie = false;
+    const unsigned long long r = j < n ? grid_units(w[j], e_s, &tie) : 0;
+    if (t == 0) {
+      first_break = nb;
+    }
+    const unsigned long long rr = block_scan_sat(r, warp_tot);
+    const unsigned long long m = m_sum + rr;
+    if (j < n && (tie || m >= (1ull << 53))) {
+      atomicMin(&first_break, t);
+    }
+    __syncthreads();
+    const int first = first_break;
+    if (t < first && j < n) {
+      ser[j] = __longlong_as_double(static_cast<long long>(base + m));
+    }
+    __syncthreads();
+    if (t == 0) {
+      const int jb = j0 + 1 + first;
+      if (first < 32 && jb < n) {
+        const int stop = min(n - 1, j0 + 128);
+        double acc = ser[jb - 1];
+        for (int q = jb; q <= stop; ++q) {
+          acc = acc + w[q];
+          ser[q] = acc;
+        }
+        s_sum = acc;
+        s_j0 = stop;
+      } else if (first < nb && jb < n) {
+        const double v = ser[jb - 1] + w[jb];
+        ser[jb] = v;
+        s_sum = v;
+        s_j0 = jb;
+      } else {
+        const int last = min(n - 1, j0 + nb);
+        s_sum = ser[last];
+        s_j0 = last;
+      }
+    }
+    __syncthreads();
+  }
+  return s_sum;
+}
 
 // The whole block resamples group g serially and counts it.
 __device__ void serial_fallback(const filter_view& f, int g, int* count) {
-  __shared__ double buf[FALLBACK_CHUNK];
   __shared__ double total;
   const int n = f.n_particles[g];
   const double* w = f.ew + f.offset[g];
   double* ser = f.pre + f.offset[g];
   int* idx = f.idx + f.offset[g];
-  double run = 0;
-  for (int base = 0; base < n; base += FALLBACK_CHUNK) {
-    const int m = min(FALLBACK_CHUNK, n - base);
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      buf[i] = w[base + i];
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll 8
-      for (int i = 0; i < m; ++i) {
-        run = run + buf[i];
-        buf[i] = run;
-      }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-      ser[base + i] = buf[i];
-    }
-    __syncthreads();
-  }
+  const double run = exact_running_sums(w, ser, n);
   if (threadIdx.x == 0) {
     total = run;
     count[g] += 1;
@@ -384,7 +548,8 @@ __device__ void serial_fallback(const filter_view& f, int g, int* count) {
   }
 }
 
-__global__ void k_fallback_count(filter_view f, int* count) {
+__global__ void __launch_bounds__(FALLBACK_THREADS)
+k_fallback_count(filter_view f, int* count) {
   const int g = blockIdx.x;
   if (!f.active[g] || f.mode[g] != MODE_RESAMPLE || !f.gflag[g]) {
     return;

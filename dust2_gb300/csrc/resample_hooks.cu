@@ -149,7 +149,7 @@ void hook_resample(hook_buffers& hb, double u, int tile_size, int serial,
   k_weights_raw<<<hb.n_tiles, tile_size, 0, s>>>(hb.f);
   k_group_given_u<<<1, 32, 0, s>>>(hb.f, u, 0, serial);
   k_resample<<<hb.n_tiles, tile_size, 0, s>>>(hb.f);
-  k_fallback_count<<<1, 256, 0, s>>>(hb.f, fallback_count);
+  k_fallback_count<<<1, FALLBACK_THREADS, 0, s>>>(hb.f, fallback_count);
   DUST2_CUDA(cudaGetLastError());
 }
 

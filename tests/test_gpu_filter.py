@@ -367,6 +367,28 @@ def test_fused_tail_is_identical(n_particles):
         assert res[0][4] == res[1][4]
 
 
+def test_resample_weight_adversarial(port):
+    """Weights that make the parallel decision ambiguous, so that the
+    serial running sum is taken (and its binade-segmented exact form is
+    exercised): equal weights, powers of two down to subnormals, exact
+    halfway cases, sparse weights and a range of 700 orders of magnitude."""
+    rs = np.random.default_rng(17)
+    cases = []
+    for n in (1000, 40000):
+        cases.append(np.ones(n))
+        cases.append(np.ldexp(1.0, -rs.integers(0, 1100, n)))
+        cases.append(rs.integers(0, 4, n) * 0.5)
+        cases.append(np.where(rs.uniform(size=n) < 0.95, 0.0,
+                              rs.uniform(size=n)))
+        cases.append(np.exp(-700 * rs.uniform(size=n)))
+        cases.append(np.ldexp(rs.integers(0, 1000, n).astype(float),
+                              rs.integers(-30, 30, n)))
+    for w in cases:
+        for u in (0.0, 0.5, rs.uniform(), 1 - 1e-12):
+            np.testing.assert_array_equal(d.resample_weight(w, u),
+                                          port.resample_weight(w, u))
+
+
 def test_resample_weight_hook(port):
     """test-filter-details.R:1-22 through the GPU kernels, including exact
     ties, where the parallel decision must defer to the serial one."""
