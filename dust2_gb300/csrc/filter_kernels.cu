@@ -6,6 +6,7 @@
 
 #include <cooperative_groups.h>
 
+#include "dust2gpu/exact_sum.hpp"
 #include "dust2gpu/math.hpp"
 #include "dust2gpu/random.hpp"
 #include "engine/device.cuh"
@@ -329,68 +330,19 @@ __global__ void k_resample(filter_view f) {
 // rounding is monotone), which the whole block finds by binary search.
 // The running sums overwrite this group's `pre` entries.
 //
-// Exact running sums in parallel.  While the running sum stays within one
-// binade [2^e, 2^(e+1)), every sum it takes is rounded to the same grid
-// of multiples of ulp = 2^(e-52), so fl(s + w) = s + ulp * r with
-// r = round(w / ulp) an integer that does not depend on s (the one
-// exception is a tie, w / ulp exactly halfway between integers, which
-// rounds to the even sum).  Within a binade the running sum is therefore
-// a prefix sum of integers, which is associative: the block scans the
-// integers r of a window of weights, and every position before the first
-// one that would leave the binade (or is a tie) gets its exact value.
-// That one step is taken with a real FP64 add, and the next window starts
+// Exact running sums in parallel (dust2gpu/exact_sum.hpp): within one
+// binade of the running sum, every step adds an integer number of grid
+// units that does not depend on the sum, so the block scans the units of
+// a window of weights, and every position before the first one that
+// leaves the binade (or is a halfway case) gets its exact value.  That
+// one step is taken with a real FP64 add, and the next window starts
 // after it.  A run of weights whose breaks come within 32 positions of
 // each other (the first steps, when the sum is small) is added one by one
 // by thread 0, which bounds the cost by about that of the plain loop.
 // A sum that is Inf, NaN or negative (weights outside the contract)
-// continues one by one.  The steps taken are the
-// reference's own, so the sums are the same bits; a group of 32,768
-// particles takes ~50 block-wide windows instead of 32,768 dependent
-// FP64 adds.
-
-__device__ __forceinline__ unsigned long long sat_add(unsigned long long a,
-                                                      unsigned long long b) {
-  const unsigned long long c = a + b;  // both <= 2^62: no wrap
-  return c > (1ull << 62) ? (1ull << 62) : c;
-}
-
-// round(w / 2^e_s) for w >= 0 as an integer, saturated at 2^62; *tie when
-// w / 2^e_s is exactly halfway between two integers.
-__device__ __forceinline__ unsigned long long grid_units(double w, int e_s,
-                                                         bool* tie) {
-  const unsigned long long wb = __double_as_longlong(w);
-  const int be = static_cast<int>(wb >> 52);
-  unsigned long long m = wb & ((1ull << 52) - 1);
-  int e_w = -1074;
-  if (be != 0) {
-    m |= 1ull << 52;
-    e_w = be - 1075;
-  }
-  *tie = false;
-  if (m == 0) {
-    return 0;
-  }
-  const int d = e_w - e_s;
-  if (d >= 0) {
-    if (d >= 62 || (m >> (62 - d)) != 0) {
-      return 1ull << 62;
-    }
-    return m << d;
-  }
-  const int sh = -d;
-  if (sh > 54) {
-    return 0;  // below half a unit (m < 2^53)
-  }
-  unsigned long long q = m >> sh;
-  const unsigned long long rem = m & ((1ull << sh) - 1);
-  const unsigned long long half = 1ull << (sh - 1);
-  if (rem > half) {
-    q += 1;
-  } else if (rem == half) {
-    *tie = true;
-  }
-  return q;
-}
+// continues one by one.  The steps taken are the reference's own, so the
+// sums are the same bits; a group of 32,768 particles takes ~50
+// block-wide windows instead of 32,768 dependent FP64 adds.
 
 // Inclusive block scan of saturating sums (blockDim.x a multiple of 32,
 // at most 1024).  Ends with the block synchronised.
@@ -402,7 +354,7 @@ __device__ unsigned long long block_scan_sat(unsigned long long v,
   for (int off = 1; off < 32; off <<= 1) {
     const unsigned long long t = __shfl_up_sync(0xffffffffu, v, off);
     if (lane >= off) {
-      v = sat_add(v, t);
+      v = exact_sum::sat_add(v, t);
     }
   }
   if (lane == 31) {
@@ -414,7 +366,7 @@ __device__ unsigned long long block_scan_sat(unsigned long long v,
     for (int off = 1; off < 32; off <<= 1) {
       const unsigned long long t = __shfl_up_sync(0xffffffffu, x, off);
       if (lane >= off) {
-        x = sat_add(x, t);
+        x = exact_sum::sat_add(x, t);
       }
     }
     if (lane < n_warps) {
@@ -423,7 +375,7 @@ __device__ unsigned long long block_scan_sat(unsigned long long v,
   }
   __syncthreads();
   if (warp > 0) {
-    v = sat_add(v, warp_tot[warp - 1]);
+    v = exact_sum::sat_add(v, warp_tot[warp - 1]);
   }
   __syncthreads();  // warp_tot may be rewritten by the next call
   return v;
@@ -450,9 +402,8 @@ __device__ double exact_running_sums(const double* w, double* ser, int n) {
     if (j0 >= n - 1) {
       break;
     }
-    const unsigned long long sb = __double_as_longlong(sum);
-    const int be = static_cast<int>(sb >> 52);
-    if (be >= 2047) {  // Inf, NaN or negative: the rest one by one
+    const exact_sum::grid gr = exact_sum::grid_of(sum);
+    if (!gr.ok) {  // Inf, NaN or negative: the rest one by one
       if (t == 0) {
         double acc = sum;
         for (int j = j0 + 1; j < n; ++j) {
@@ -464,28 +415,21 @@ __device__ double exact_running_sums(const double* w, double* ser, int n) {
       __syncthreads();
       break;
     }
-    // sum = (base + m_sum) as bits, with the grid 2^e_s of its binade
-    // (subnormals share the grid of the first normal binade)
-    const int bep = be < 1 ? 1 : be;
-    const int e_s = bep - 1075;
-    const unsigned long long base = static_cast<unsigned long long>(bep - 1)
-      << 52;
-    const unsigned long long m_sum = sb - base;
     const int j = j0 + 1 + t;
     bool tie = false;
-    const unsigned long long r = j < n ? grid_units(w[j], e_s, &tie) : 0;
+    const unsigned long long r =
+      j < n ? exact_sum::grid_units(w[j], gr.e_grid, &tie) : 0;
     if (t == 0) {
       first_break = nb;
     }
-    const unsigned long long rr = block_scan_sat(r, warp_tot);
-    const unsigned long long m = m_sum + rr;
-    if (j < n && (tie || m >= (1ull << 53))) {
+    const unsigned long long m = gr.count + block_scan_sat(r, warp_tot);
+    if (j < n && exact_sum::is_break(m, tie)) {
       atomicMin(&first_break, t);
     }
     __syncthreads();
     const int first = first_break;
     if (t < first && j < n) {
-      ser[j] = __longlong_as_double(static_cast<long long>(base + m));
+      ser[j] = exact_sum::grid_value(gr, m);
     }
     __syncthreads();
     if (t == 0) {
