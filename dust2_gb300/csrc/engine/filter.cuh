@@ -20,7 +20,8 @@
 //   4. k_resample      one thread per particle: systematic resampling
 //                      target uu_i = sum*u/n + i*sum/n and a search of the
 //                      prefix sums (filter_details.hpp:45-74).
-//   5. k_fallback      one block per flagged group: the serial algorithm.
+//   5. k_fallback      one block per flagged group: the serial algorithm
+//                      (its running sum reproduced exactly in parallel).
 //   6. k_reorder       gather of the resampled state (discrete/system.hpp
 //                      :170-181).
 //
@@ -35,8 +36,9 @@
 // a rigorous, position-dependent bound on the difference between the
 // serial and the parallel prefix sums (see k_resample); a decision is
 // accepted only when both neighbouring prefix sums are farther than that
-// from the target, otherwise the whole group is recomputed serially
-// (step 5), which is the reference algorithm verbatim.  The
+// from the target, otherwise the whole group is recomputed with the
+// reference algorithm (step 5), whose left-to-right running sum the block
+// reproduces bit for bit (exact_running_sums in filter_kernels.cu).  The
 // log-likelihood uses the parallel total; it matches the serial one to
 // better than n u relative (u = 2^-53).
 //
