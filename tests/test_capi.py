@@ -23,6 +23,21 @@ def test_library_exports_every_declared_symbol(built):
     assert lib.dust2_gb300_abi_version() == 1
 
 
+def test_ctypes_prototypes_match_header_arity():
+    """Every C ABI declaration and its ctypes prototype take the same number
+    of arguments (catches a binding that drifted from the header)."""
+    import re
+    text = _lib.HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    decls = re.findall(r"\b(dust2_gb300_[a-z_0-9]+)\s*\(([^;{]*?)\)\s*;",
+                       text, flags=re.S)
+    assert len(decls) == len(_lib._SIGNATURES)
+    for name, params in decls:
+        p = params.strip()
+        n = 0 if p in ("", "void") else len(p.split(","))
+        assert len(_lib._SIGNATURES[name][1]) == n, name
+
+
 def test_device_count_without_gpu_is_reported(built):
     assert d.device_count() >= 0
 
