@@ -1,14 +1,27 @@
-"""Benchmark: batched SIR particle filter, particle-steps/s on one GB300.
+"""Benchmark of the dust2 hot path on one GB300.
 
-Workload (default, `--workload sir_batched`): 64 parameter groups of the
-stochastic SIR model (beta ~ U(0.1, 0.5), gamma ~ U(0.05, 0.2), N = 1e6,
-I0 ~ U{1..100}), uneven particle counts round(2^U(9, 15)) per group from
-seed 1, 200 daily observations per group simulated from the model plus
-Poisson noise, dt = 0.25 (4 steps per observation), one likelihood
-evaluation of all groups per step.  Data are synthetic (the model itself
-generates them; there is no external dataset).
+Default workload (`--workload serve_seir`): filter likelihoods of the
+age-structured stochastic SEIR (16 ages, 96 FP64 states, dt 0.25,
+negative-binomial compare) requested by 64 concurrent MCMC-chain clients:
+first requests a Poisson stream at 200/s, then one request outstanding
+per client with exponential think times; per client a session with
+round(2^U(9, 15)) particles and U{50..365} days of data (seed 11), a new
+R0 ~ U(1.2, 3) per request.  A step is 16 requests (20 steps: 5 per
+client).  The line reports the served engine (continuous batching on one
+likelihood server) against the plain path (the same requests one by one
+through dust_likelihood_run), p50/p99 latency of both, the plain path's
+per-request share of the device's full rate (and so the most any batching
+could gain), the roofline of the SEIR step kernel and the CPU path on a
+bounded sample.
 
-Reported numbers (one JSON line on rank 0):
+Other workloads (`--workload`): sir_batched (64 SIR groups, uneven
+particle counts round(2^U(9, 15)), 200 observations), seir_batched (32
+SEIR groups x 8192 particles, 365 observations), sir_small (one SIR group
+of 1000 particles, 100 observations), ode_batched (262,144 sirode
+instances, dopri5 to t = 200).  Data are synthetic everywhere: the model
+itself generates them from fixed seeds.
+
+Filter workloads report:
   value   particle-steps/s of whole likelihood runs, device-timed with CUDA
           events on the filter's stream, inputs resident on the device, L2
           flushed (256 MB write) between timed runs;
@@ -19,12 +32,13 @@ Reported numbers (one JSON line on rank 0):
           FP64 pipe: executed FP64 operations per particle-step (ncu SASS
           counters of this kernel, stated in the constant below) times the
           particle-steps of one launch, over the kernel's device time
-          measured live with CUDA events inside the timed runs; peak from a
-          DFMA microbenchmark run in this process;
+          measured live with CUDA events; peak from a DFMA microbenchmark
+          run in this process; plus the HBM roofline of the reorder gather;
   cpu_baseline  the CPU restatement of dust2's engine (OpenMP over all
           host cores) on a bounded sample of the same workload.
 
-`--impl reference` times that CPU implementation alone (the reference arm).
+`--impl reference` times that CPU implementation alone (the reference arm),
+with inputs built by the oracle, so it never loads the CUDA library.
 Multi-GPU (torchrun) runs independent replicas, one per GPU: the path has
 no cross-group exchange.
 """
@@ -75,6 +89,34 @@ def traffic_per_launch(workload, units_per_launch):
     return None if b is None else b * units_per_launch
 
 
+def hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of the GB300s, or the
+    earlier fallback measurement when the driver's file is absent."""
+    try:
+        with open(ROOT / "MEASURED_PEAKS.json") as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def reorder_roofline(n_particles, n_state, ms, n_launches):
+    """HBM roofline of the reorder gather (discrete/system.hpp:170-181):
+    per particle n_state doubles read and written plus its 4-byte source
+    index, over the mean CUDA-event time of one launch.  None when no
+    launch was timed (the fused cluster tail)."""
+    if n_launches <= 0 or ms <= 0:
+        return None
+    per_launch = ms / n_launches
+    nbytes = n_particles * (16 * n_state + 4)
+    achieved = nbytes / (per_launch * 1e-3) / 1e9
+    peak, source = hbm_peak()
+    return {"bound": "hbm", "kernel": "k_reorder", "bytes_per_launch": nbytes,
+            "launch_ms": per_launch, "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": f"{source} (MEASURED_PEAKS.json hbm_gbs: "
+                           "a STREAM-style copy)"}
+
+
 def pipe_roofline(workload, units_per_s, peak_tflops):
     """Useful FP64-pipe thread instructions per second against the pipe's
     peak (peak DFMA flops / 2)."""
@@ -90,10 +132,10 @@ STEPS_PER_OBS = 4  # dt = 0.25, daily observations
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", default="sir_batched",
+    p.add_argument("--workload", default="serve_seir",
                    choices=["sir_batched", "sir_small", "seir_batched",
                             "serve_seir", "ode_batched"])
     p.add_argument("--hbm-budget", type=float, default=16e9,
@@ -201,21 +243,34 @@ def fp64_peak_tflops():
 N_STATE = {"sir_cases": 4, "sir": 5, "seir_age": 96}
 
 
-def build_workload(name, simulate):
+def build_workload(name, simulate, packer=None):
     from dust2_gb300 import workloads
     if name == "sir_batched":
-        w = workloads.sir_batched(simulate)
+        w = workloads.sir_batched(simulate, packer=packer)
         w["system"] = "sir_cases"
     elif name == "seir_batched":
-        w = workloads.seir_batched(simulate)
+        w = workloads.seir_batched(simulate, packer=packer)
         w["system"] = "seir_age"
     else:
-        w = workloads.sir_small(simulate)
+        w = workloads.sir_small(simulate, packer=packer)
         w["data"] = w["data"].reshape(-1, 1)
         w["n_particles"] = [w["n_particles"]]
         w["system"] = "sir_cases"
     w["n_state"] = N_STATE[w["system"]]
     return w
+
+
+def filter_config(args, w, world=1):
+    """The config object of both arms of the filter benchmarks."""
+    npg = w["n_particles"]
+    n_obs = w["times"].size
+    return {"workload": args.workload, "system": w["system"],
+            "n_groups": len(npg), "n_particles_total": sum(npg),
+            "n_observations": n_obs,
+            "steps_per_observation": STEPS_PER_OBS,
+            "particle_steps_per_step": sum(npg) * n_obs * STEPS_PER_OBS,
+            "l2": "flushed (256 MB write) between timed steps",
+            "parallelism": f"replicas x{world}"}
 
 
 def data_columns(w):
@@ -229,18 +284,17 @@ def data_columns(w):
 
 def run_cpu(w, n_groups, n_threads, n_runs=1):
     """Run the CPU oracle on the first n_groups groups of the workload;
-    returns (seconds per run, particle-steps per run)."""
+    returns (seconds per run, particle-steps per run).  Inputs are packed
+    and seeded by the oracle itself."""
     from oracle import pyoracle
-    import dust2_gb300 as d
     port = pyoracle.port_timing()
     npg = w["n_particles"][:n_groups]
     G_all = len(w["n_particles"])
-    gen = d.Generator(w["system"])
-    npar = gen.n_pars
+    npar = np.asarray(w["pars"]).size // G_all
     pars = np.asarray(w["pars"]).reshape(G_all, npar)[:n_groups].ravel()
     data = np.asarray(w["data"]).reshape(w["times"].size, G_all)[:, :n_groups]
     n_streams = sum(n + 2 for n in npg)
-    rng = np.frombuffer(d.rng_streams(n_streams, w["seed"]), dtype="<u8")
+    rng = pyoracle.rng_streams(n_streams, w["seed"])
     t0 = time.perf_counter()
     port.filter_run(w["system"], pars, npg, 0.0, w["times"], data.ravel(),
                     n_groups, w["dt"], rng, n_runs=n_runs,
@@ -250,11 +304,9 @@ def run_cpu(w, n_groups, n_threads, n_runs=1):
     return dt, ps
 
 
-def cpu_baseline(w, target_seconds):
-    from oracle import pyoracle
-    port = pyoracle.port_timing()
-    threads = port.max_threads()
-    # calibrate on the first group, then grow the sample to the target
+def cpu_sample_groups(w, target_seconds, threads):
+    """How many leading groups of the workload take about target_seconds
+    on the CPU (calibrated on the first group)."""
     t1, ps1 = run_cpu(w, 1, threads)
     rate = ps1 / max(t1, 1e-9)
     G = len(w["n_particles"])
@@ -264,13 +316,24 @@ def cpu_baseline(w, target_seconds):
     while n_groups < G and total / rate < target_seconds:
         total += per_group[n_groups]
         n_groups += 1
+    return n_groups
+
+
+def cpu_sample_text(w, n_groups):
+    G = len(w["n_particles"])
+    return (f"groups 1-{n_groups} of {G} ({sum(w['n_particles'][:n_groups])}"
+            f" particles), all {w['times'].size} observations, one "
+            "likelihood evaluation")
+
+
+def cpu_baseline(w, target_seconds):
+    from oracle import pyoracle
+    threads = pyoracle.port_timing().max_threads()
+    n_groups = cpu_sample_groups(w, target_seconds, threads)
     t, ps = run_cpu(w, n_groups, threads)
-    sample = (f"groups 1-{n_groups} of {G} ({sum(w['n_particles'][:n_groups])}"
-              f" particles), all {w['times'].size} observations, one "
-              "likelihood evaluation")
     return {"value": ps / t, "unit": "particle-steps/s", "cores": threads,
-            "kind": "port", "sample": sample, "seconds": t,
-            "math": CPU_MATH}
+            "kind": "port", "sample": cpu_sample_text(w, n_groups),
+            "seconds": t, "math": CPU_MATH}
 
 
 def gpu_simulate_factory():
@@ -387,6 +450,10 @@ def gpu_arm(args, rank, world, local):
     _lib.check(lib.dust2_gb300_filter_kernel_times(
         h, ctypes.byref(step_ms), ctypes.byref(n_step), ctypes.byref(run_ms),
         ctypes.byref(n_run)))
+    reorder_ms = ctypes.c_double()
+    n_reorder = ctypes.c_int64()
+    _lib.check(lib.dust2_gb300_filter_reorder_times(
+        h, ctypes.byref(reorder_ms), ctypes.byref(n_reorder)))
     _lib.check(lib.dust2_gb300_filter_set_timing(h, 0))
     ms = float(np.mean(elapsed))
     ms_max = max_over_ranks(ms, world, "cuda")
@@ -445,12 +512,7 @@ def gpu_arm(args, rank, world, local):
             "ms_per_step": ms_max, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (simulated by the model, seeded)",
-            "config": {"workload": args.workload, "n_groups": n_groups,
-                       "n_particles_total": n_total, "n_observations": n_obs,
-                       "steps_per_observation": STEPS_PER_OBS,
-                       "particle_steps_per_step": particle_steps,
-                       "l2": "flushed (256 MB write) between timed steps",
-                       "parallelism": f"replicas x{world}"},
+            "config": filter_config(args, w, world),
             "e2e": {"value": particle_steps * world / e2e_max,
                     "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_max},
@@ -462,6 +524,8 @@ def gpu_arm(args, rank, world, local):
             "clocks": clock_info,
             "roofline": roofline,
             "serial_fallbacks": d.dust_likelihood_serial_fallbacks(obj),
+            "reorder_roofline": reorder_roofline(
+                n_total, w["n_state"], reorder_ms.value, n_reorder.value),
         }
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
@@ -474,37 +538,111 @@ def percentile(x, q):
     return float(np.percentile(np.asarray(x, dtype=float), q))
 
 
+# A step of the serving benchmark is this many likelihood requests; they
+# are spread over the clients in turn, so 20 steps give each of the 64
+# clients 5 requests.
+REQUESTS_PER_STEP = 16
+SERVE_METRIC = ("filter particle-steps/s and p50/p99 latency, served vs "
+                "plain GPU")
+
+
+def serve_workload(simulate, steps, packer=None):
+    """The serving workload with REQUESTS_PER_STEP * steps requests:
+    client i makes counts[i] of them (the first clients one more when
+    they do not divide evenly)."""
+    from dust2_gb300 import workloads
+    n_clients = 64
+    base, extra = divmod(REQUESTS_PER_STEP * steps, n_clients)
+    counts = [base + (1 if i < extra else 0) for i in range(n_clients)]
+    w = workloads.serving_clients(simulate, n_clients=n_clients,
+                                  rounds=max(1, max(counts)), packer=packer)
+    w["counts"] = counts
+    w["particle_steps"] = sum(n * c["particle_steps"]
+                              for n, c in zip(counts, w["clients"]))
+    return w
+
+
+def serve_config(args, w):
+    """The config object of both arms of the serving benchmark."""
+    clients = w["clients"]
+    return {"workload": "serve_seir", "system": "seir_age (16 ages, 96 "
+            "states, dt 0.25, negative-binomial compare)",
+            "clients": len(clients), "requests": sum(w["counts"]),
+            "requests_per_step": REQUESTS_PER_STEP,
+            "requests_per_client": [min(w["counts"]), max(w["counts"])],
+            "arrival_rate_per_s": w["rate"],
+            "particles": [c["n_particles"] for c in clients],
+            "days": [int(c["data"]["time"].size) for c in clients],
+            "particle_steps": w["particle_steps"],
+            "hbm_budget_bytes": args.hbm_budget,
+            "l2": "not flushed: a continuous request stream; each "
+                  "request's state (0.4-50 MB) is resident between requests",
+            "parallelism": "1 GPU, one server"}
+
+
+def seir_device_rate(simulate, n_obs=30):
+    """Particle-steps/s of the plain filter when it fills the device: 32
+    SEIR groups x 8192 particles (the batched SEIR workload) over its
+    first n_obs observations, through dust_likelihood_run."""
+    import dust2_gb300 as d
+    from dust2_gb300 import workloads
+    w = workloads.seir_batched(simulate, n_obs=n_obs)
+    w["system"] = "seir_age"
+    obj = d.dust_filter_create(d.seir_age(), 0, data_columns(w),
+                               n_particles=w["n_particles"], dt=w["dt"],
+                               seed=w["seed"])
+    d.dust_likelihood_run(obj, w["plist"])
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        d.dust_likelihood_run(obj, w["plist"])
+        times.append(time.perf_counter() - t0)
+    ps = sum(w["n_particles"]) * n_obs * STEPS_PER_OBS
+    return {"value": ps / min(times), "unit": "particle-steps/s",
+            "workload": f"seir_age 32 groups x 8192 particles, first "
+                        f"{n_obs} observations, dust_likelihood_run"}
+
+
 def serve_arm(args, rank, world, local):
     """Served likelihoods vs the plain path on the serving workload.
 
-    `--steps K` is the number of requests per client (each client is an
-    MCMC chain: one request outstanding, the next after its result and an
-    exponential think time); `--warmup W` warm-up requests run first on a
-    separate session.  Served: every client's session is open on one
-    likelihood server and clients submit and wait from their own threads
-    in real time.  Plain: the same requests, in arrival order, one by one
-    through dust_likelihood_run on one-group filters (service times
-    measured; the arrival process is replayed against the single plain
-    executor, which is serial, to get each request's queueing delay).
-    Both arms include host parameters in and host log-likelihoods out."""
-    import heapq
+    64 clients (MCMC chains) each keep one request outstanding: the first
+    requests arrive as a Poisson stream at 200/s, and after each result a
+    client waits an exponential think time before its next request.  A
+    benchmark step is REQUESTS_PER_STEP requests.
+
+    Served: every client's session is open on one likelihood server, and
+    each client thread submits and waits in real time.  Plain: the same
+    requests, submitted in real time by the same client threads, run one
+    by one in arrival order by a single executor thread through
+    dust_likelihood_run on one-group filters (one per client).  Latency
+    is submit to result on both arms, and both include host parameters
+    in and host log-likelihoods out.  The plain arm's per-request rate is
+    compared with the device's full rate on this system (the batched SEIR
+    filter) to bound what any batching can gain over it."""
+    import queue
 
     import torch
     torch.cuda.set_device(local)
     import __graft_entry__
     __graft_entry__.build()
     import dust2_gb300 as d
-    from dust2_gb300 import workloads
 
-    rounds = args.steps
-    w = workloads.serving_clients(gpu_simulate_factory(), rounds=rounds)
+    simulate = gpu_simulate_factory()
+    w = serve_workload(simulate, args.steps)
     clients = w["clients"]
+    counts = w["counts"]
     C = len(clients)
+    total_ps = w["particle_steps"]
     gen = d.seir_age()
+    c0 = clients[0]
+
+    clocks = ClockSampler(local)
+    clocks.start()
+
+    # served arm
     server = d.dust_likelihood_server(gen, hbm_budget=args.hbm_budget,
                                       max_sessions=2 * C)
-    # warm-up (module load, first launches) on a separate session
-    c0 = clients[0]
     warm = server.open(c0["pars"][0], c0["data"], 512, dt=w["dt"], seed=1)
     for _ in range(args.warmup):
         server.likelihood(warm, c0["pars"][0])
@@ -513,46 +651,44 @@ def serve_arm(args, rank, world, local):
                        seed=c["seed"]) for c in clients]
     server.set_timing(True)
     st0 = server.stats()
-    served_ll = [[None] * rounds for _ in range(C)]
+    served_ll = [[None] * n for n in counts]
     served_lat = []
     lock = threading.Lock()
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.5)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    t_end = [0.0] * C
+    t_end = [t0] * C
 
-    def client(i):
+    def served_client(i):
         c = clients[i]
         delay = t0 + w["first_arrival"][i] - time.perf_counter()
         if delay > 0:
             time.sleep(delay)
-        for r in range(rounds):
+        for r in range(counts[i]):
             ticket = server.submit(ids[i], c["pars"][r])
             ll, lat = server.wait(ticket)
             with lock:
                 served_ll[i][r] = ll
                 served_lat.append(lat)
             t_end[i] = time.perf_counter()
-            if r + 1 < rounds:
+            if r + 1 < counts[i]:
                 time.sleep(w["think"][i, r])
 
-    threads = [threading.Thread(target=client, args=(i,)) for i in range(C)]
+    threads = [threading.Thread(target=served_client, args=(i,))
+               for i in range(C)]
     for th in threads:
         th.start()
     for th in threads:
         th.join()
     served_s = max(t_end) - t0
-    clock_info = clocks.stop()
     st = server.stats()
-    total_ps = rounds * sum(c["particle_steps"] for c in clients)
     served_value = total_ps / served_s
     step_ms = st["step_kernel_ms"] - st0["step_kernel_ms"]
     launches = int(st["kernel_launches"] - st0["kernel_launches"])
+    server_info = {k: st[k] for k in ("device_steps", "requests_done",
+                                      "max_running", "particle_capacity")}
     server.free()
 
-    # plain arm
+    # plain arm: one filter per client, one executor
     objs = [d.dust_filter_create(gen, 0, c["data"],
                                  n_particles=c["n_particles"], dt=w["dt"],
                                  seed=c["seed"]) for c in clients]
@@ -560,30 +696,73 @@ def serve_arm(args, rank, world, local):
                                 dt=w["dt"], seed=1)
     for _ in range(args.warmup):
         d.dust_likelihood_run(wobj, c0["pars"][0])
-    heap = [(float(w["first_arrival"][i]), i, 0) for i in range(C)]
-    heapq.heapify(heap)
-    now = 0.0
+    for i, c in enumerate(clients):
+        if counts[i] > 0:
+            # allocate each filter and capture its graph before the timed
+            # region, then put its generators back where they started, so
+            # that its requests see the streams the served session sees
+            words = d.dust_likelihood_rng_state(objs[i])
+            d.dust_likelihood_run(objs[i], c["pars"][0])
+            d.dust_likelihood_set_rng_state(objs[i], words)
+    plain_ll = [[None] * n for n in counts]
     plain_lat = []
-    plain_ll = [[None] * rounds for _ in range(C)]
-    service = []
-    while heap:
-        arrival, i, r = heapq.heappop(heap)
-        start = max(now, arrival)
-        torch.cuda.synchronize()
-        a = time.perf_counter()
-        ll = d.dust_likelihood_run(objs[i], clients[i]["pars"][r])
-        svc = time.perf_counter() - a
-        plain_ll[i][r] = float(np.ravel(ll)[0])
-        service.append(svc)
-        now = start + svc
-        plain_lat.append(now - arrival)
-        if r + 1 < rounds:
-            heapq.heappush(heap, (now + float(w["think"][i, r]), i, r + 1))
-    plain_s = now
+    service = []  # (particle-steps, seconds) per request
+    todo = queue.Queue()
+    n_requests = sum(counts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    t_end = [t0] * C
+
+    def executor():
+        for _ in range(n_requests):
+            i, r, box = todo.get()
+            a = time.perf_counter()
+            ll = d.dust_likelihood_run(objs[i], clients[i]["pars"][r])
+            b = time.perf_counter()
+            box["ll"] = float(np.ravel(ll)[0])
+            service.append((clients[i]["particle_steps"], b - a))
+            box["done"].set()
+
+    def plain_client(i):
+        delay = t0 + w["first_arrival"][i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        for r in range(counts[i]):
+            box = {"done": threading.Event()}
+            submitted = time.perf_counter()
+            todo.put((i, r, box))
+            box["done"].wait()
+            done = time.perf_counter()
+            with lock:
+                plain_ll[i][r] = box["ll"]
+                plain_lat.append(done - submitted)
+            t_end[i] = done
+            if r + 1 < counts[i]:
+                time.sleep(w["think"][i, r])
+
+    ex = threading.Thread(target=executor)
+    ex.start()
+    threads = [threading.Thread(target=plain_client, args=(i,))
+               for i in range(C)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    ex.join()
+    plain_s = max(t_end) - t0
+    clock_info = clocks.stop()
     plain_value = total_ps / plain_s
     same = all(np.array_equal(np.array(a, dtype=float),
                               np.array(b, dtype=float))
                for a, b in zip(served_ll, plain_ll))
+
+    # the device's full rate on this system, and each plain request's
+    # share of it
+    dev = seir_device_rate(simulate)
+    rate = np.array([ps / s for ps, s in service])
+    util = rate / dev["value"]
+    busy = sum(ps for ps, _ in service) / sum(s for _, s in service)
+    weighted = busy / dev["value"]
 
     ops = FP64_OPS_PER_PARTICLE_STEP.get("seir_batched")
     peak = fp64_peak_tflops()
@@ -592,45 +771,64 @@ def serve_arm(args, rank, world, local):
                 if ops is not None and in_kernel_rate else None)
     n_par = gen.n_pars
     line = {
-        "metric": "served filter particle-steps/s",
+        "metric": SERVE_METRIC,
         "value": served_value, "unit": "particle-steps/s", "n_gpus": 1,
-        "steps": rounds, "warmup": args.warmup,
-        "ms_per_step": served_s * 1e3 / rounds, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": served_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64",
         "data": "synthetic (simulated by the model, seeded)",
-        "config": {"workload": "serve_seir", "clients": C,
-                   "requests": C * rounds, "arrival_rate_per_s": w["rate"],
-                   "particles": [c["n_particles"] for c in clients],
-                   "particle_steps": total_ps,
-                   "hbm_budget_bytes": args.hbm_budget,
-                   "l2": "not flushed: a continuous request stream",
-                   "parallelism": "1 GPU, one server"},
+        "config": serve_config(args, w),
         "latency_s": {"served": {"p50": percentile(served_lat, 50),
                                  "p99": percentile(served_lat, 99)},
                       "plain": {"p50": percentile(plain_lat, 50),
                                 "p99": percentile(plain_lat, 99)}},
         "plain": {"value": plain_value, "unit": "particle-steps/s",
-                  "seconds": plain_s,
-                  "mean_service_s": float(np.mean(service))},
+                  "seconds": plain_s, "busy_rate": busy,
+                  "mean_service_s": float(np.mean([s for _, s in service]))},
+        "served": {"value": served_value, "seconds": served_s,
+                   "in_step_kernel_rate": in_kernel_rate},
         "served_over_plain": served_value / plain_value,
         "results_equal_plain": bool(same),
-        "server": {k: st[k] for k in ("device_steps", "requests_done",
-                                      "max_running", "particle_capacity")},
+        "device_rate": dev,
+        "plain_utilisation": {
+            "weighted": weighted,
+            "p10": percentile(util, 10), "p50": percentile(util, 50),
+            "p90": percentile(util, 90),
+            "note": "each plain request's particle-steps/s over the "
+                    "device rate; weighted = all plain particle-steps "
+                    "over all plain service time, over the device rate"},
+        "served_over_plain_bound": 1.0 / weighted,
+        "served_over_device_rate": served_value / dev["value"],
+        "server": server_info,
         "e2e": {"value": served_value, "unit": "particle-steps/s",
-                "h2d_bytes_per_step": C * n_par * 8,
-                "d2h_bytes_per_step": C * 8},
+                "h2d_bytes_per_step": REQUESTS_PER_STEP * n_par * 8,
+                "d2h_bytes_per_step": REQUESTS_PER_STEP * 8,
+                "note": "the served value is already end to end: clients "
+                        "submit host parameters and read host "
+                        "log-likelihoods through the server's C ABI"},
         "gpu_launches": launches,
         "clocks": clock_info,
         "roofline": {
             "bound": "fp64", "kernel": "k_served_step_compare<seir_age>",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": None if achieved is None else achieved / peak,
-            "traffic": None,
+            "traffic": traffic_per_launch(
+                "seir_batched",
+                total_ps / max(1, server_info["device_steps"])),
+            "traffic_source": "ncu dram bytes per particle-step of the SEIR "
+                              "step kernel (batched SEIR filter) times the "
+                              "mean particle-steps of one tick",
+            "peak_source": "measured in-process: DFMA-chain microbenchmark "
+                           "(dust2_gb300_fp64_peak); MEASURED_PEAKS.json "
+                           "has no FP64 entry",
             "step_kernel_share": step_ms * 1e-3 / served_s,
             "fp64_pipe": pipe_roofline("seir_batched", in_kernel_rate, peak),
             "flops_basis": "executed FP64 ops per particle-step of the "
-                           "SEIR step kernel (ncu, seir_batched)"},
+                           "SEIR step kernel (ncu SASS dadd+dmul+2*dfma)"},
     }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = serve_cpu_baseline(w, args.cpu_seconds)
     print(json.dumps(line), flush=True)
 
 
@@ -674,7 +872,17 @@ def ode_cpu_baseline(w, target_seconds):
             "kind": "port", "math": CPU_MATH,
             "sample": f"instances 1-{n} of {w['n_groups']}, integrated "
                       f"0..200 with {w['times'].size} outputs",
-            "seconds": t}
+            "seconds": t, "instances": n}
+
+
+def ode_config(w):
+    """The config object of both arms of the dopri5 benchmark."""
+    return {"workload": "ode_batched", "system": "sirode",
+            "instances": w["n_groups"], "outputs": int(w["times"].size),
+            "rtol": 1e-6, "atol": 1e-6,
+            "l2": "flushed (256 MB write) between timed steps; outputs "
+                  f"{w['n_groups'] * w['times'].size * 40 / 1e9:.1f} GB",
+            "parallelism": "1 GPU"}
 
 
 def ode_arm(args, rank, world, local):
@@ -765,14 +973,10 @@ def ode_arm(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded parameters)",
-        "config": {"workload": "ode_batched", "instances": G,
-                   "outputs": int(times.size), "rtol": 1e-6, "atol": 1e-6,
-                   "dopri5_steps_per_step": steps,
-                   "accepted": int(na.sum()), "rejected": int(nr.sum()),
-                   "steps_per_instance": [int(ns.min()), int(ns.max())],
-                   "l2": "flushed (256 MB write) between timed steps; "
-                         "outputs 2.1 GB",
-                   "parallelism": "1 GPU"},
+        "config": ode_config(w),
+        "dopri5": {"steps_per_step": steps, "accepted": int(na.sum()),
+                   "rejected": int(nr.sum()),
+                   "steps_per_instance": [int(ns.min()), int(ns.max())]},
         "e2e": {"value": steps / e2e_s, "unit": "dopri5 steps/s",
                 "h2d_bytes_per_step": times.size * 8,
                 "d2h_bytes_per_step": n_out * 8, "seconds_per_step": e2e_s},
@@ -795,44 +999,46 @@ def ode_arm(args, rank, world, local):
 def reference_arm(args, rank, world):
     """The CPU implementation of the path on the host cores (the oracle
     port of dust2's engine; dust2's own sources are not present on the
-    benchmark machine)."""
+    benchmark machine).  Inputs are built, packed and seeded by the
+    oracle: this arm never loads the CUDA library."""
     if rank != 0:
         return
-    import __graft_entry__  # noqa: F401
     from oracle import build as oracle_build
     oracle_build.build_port()
-    from dust2_gb300 import build as engine_build
-    engine_build.build()
     from oracle import pyoracle
 
     port = pyoracle.port_timing()
     threads = port.max_threads()
-    metric, unit = "filter particle-steps/s", "particle-steps/s"
+    unit = "particle-steps/s"
     if args.workload == "ode_batched":
         from dust2_gb300 import workloads
-        w = workloads.sirode_batched()
+        w = workloads.sirode_batched(n_instances=args.ode_instances)
         base = ode_cpu_baseline(w, args.cpu_seconds)
-        n_inst = int(base["sample"].split("-")[1].split(" ")[0])
+        n_inst = base["instances"]
 
         def one():
-            t, steps = ode_cpu(w, n_inst, threads)
-            return t, steps
+            return ode_cpu(w, n_inst, threads)
         metric, unit = "dopri5 steps/s", "dopri5 steps/s"
+        config = ode_config(w)
     elif args.workload == "serve_seir":
-        from dust2_gb300 import workloads
-        w = workloads.serving_clients(oracle_simulate(), rounds=1)
-        clients, base = serve_cpu_sample(w, args.cpu_seconds, threads)
+        w = serve_workload(oracle_simulate(), args.steps,
+                           packer=pyoracle.pack_pars)
+        picks, base = serve_cpu_sample(w, args.cpu_seconds, threads)
 
         def one():
-            return serve_cpu_run(w, clients, threads)
-        metric = "served filter particle-steps/s"
+            return serve_cpu_run(w, picks, threads)
+        metric = SERVE_METRIC
+        config = serve_config(args, w)
     else:
-        w = build_workload(args.workload, oracle_simulate())
-        base = cpu_baseline(w, args.cpu_seconds)
-        n_groups = int(base["sample"].split("-")[1].split(" ")[0])
+        w = build_workload(args.workload, oracle_simulate(),
+                           packer=pyoracle.pack_pars)
+        n_groups = cpu_sample_groups(w, args.cpu_seconds, threads)
+        base = {"sample": cpu_sample_text(w, n_groups)}
 
         def one():
             return run_cpu(w, n_groups, threads)
+        metric = "filter particle-steps/s"
+        config = filter_config(args, w, world)
     for _ in range(args.warmup):
         one()
     times = []
@@ -848,61 +1054,89 @@ def reference_arm(args, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (simulated by the model, seeded)",
-        "config": {"workload": args.workload},
+        "config": config,
         "cpu_baseline": {"value": value, "unit": unit,
                          "cores": threads, "kind": "port",
                          "sample": base["sample"], "math": CPU_MATH},
         "e2e": {"value": value, "unit": unit,
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "native_so_loaded": native_library_loaded(),
     }
     print(json.dumps(line), flush=True)
 
 
-def serve_cpu_run(w, clients, threads):
-    """The first request of each listed client, one by one, on the CPU
-    oracle (the reference's engine restated; OpenMP over particles)."""
+def native_library_loaded():
+    """Whether this process has mapped the CUDA engine's library."""
+    try:
+        with open("/proc/self/maps") as f:
+            return "libdust2_gb300" in f.read()
+    except OSError:
+        return None
+
+
+def serve_cpu_inputs(w, picks):
+    """Packed parameters, data and generator words of requests (client,
+    request) of the serving workload, built by the oracle."""
     from oracle import pyoracle
-    import dust2_gb300 as d
-    port = pyoracle.port_timing()
-    gen = d.Generator("seir_age")
-    total = 0
-    t0 = time.perf_counter()
-    for i in clients:
+    out = []
+    for i, r in picks:
         c = w["clients"][i]
         n = c["n_particles"]
-        pars = gen.pack_pars(c["pars"][0])
-        data = np.asarray(c["data"]["incidence"], dtype=float)
-        rng = np.frombuffer(d.rng_streams(n + 2, c["seed"]), dtype="<u8")
-        port.filter_run("seir_age", pars, [n], 0.0, c["data"]["time"], data,
-                        1, w["dt"], rng, n_runs=1, n_state=96,
-                        n_threads=threads)
-        total += c["particle_steps"]
+        out.append((pyoracle.pack_pars("seir_age", c["pars"][r]),
+                    np.asarray(c["data"]["incidence"], dtype=float),
+                    c["data"]["time"], n,
+                    pyoracle.rng_streams(n + 2, c["seed"]),
+                    c["particle_steps"]))
+    return out
+
+
+def serve_cpu_run(w, picks, threads):
+    """Requests (client, request) of the serving workload, one by one, on
+    the CPU oracle (the reference's engine restated; OpenMP over
+    particles); returns (seconds, particle-steps)."""
+    from oracle import pyoracle
+    port = pyoracle.port_timing()
+    inputs = serve_cpu_inputs(w, picks)
+    total = 0
+    t0 = time.perf_counter()
+    for pars, data, times, n, rng, ps in inputs:
+        port.filter_run("seir_age", pars, [n], 0.0, times, data, 1, w["dt"],
+                        rng, n_runs=1, n_state=96, n_threads=threads)
+        total += ps
     return time.perf_counter() - t0, total
 
 
 def serve_cpu_sample(w, target_seconds, threads):
-    """Clients (in order) whose first requests take about target_seconds
-    on the CPU."""
-    t, ps = serve_cpu_run(w, [0], threads)
+    """The first requests of the clients, in order, that take about
+    target_seconds on the CPU (calibrated on the first)."""
+    t, ps = serve_cpu_run(w, [(0, 0)], threads)
     rate = ps / max(t, 1e-9)
-    chosen, total = [0], ps
+    picks, total = [(0, 0)], ps
     for i in range(1, len(w["clients"])):
         if total / rate >= target_seconds:
             break
-        chosen.append(i)
+        picks.append((i, 0))
         total += w["clients"][i]["particle_steps"]
-    base = {"sample": f"first requests of clients 1-{len(chosen)} of "
+    base = {"sample": f"first requests of clients 1-{len(picks)} of "
                       f"{len(w['clients'])}, one by one"}
-    return chosen, base
+    return picks, base
+
+
+def serve_cpu_baseline(w, target_seconds):
+    from oracle import pyoracle
+    threads = pyoracle.port_timing().max_threads()
+    picks, base = serve_cpu_sample(w, target_seconds, threads)
+    t, ps = serve_cpu_run(w, picks, threads)
+    return {"value": ps / t, "unit": "particle-steps/s", "cores": threads,
+            "kind": "port", "sample": base["sample"], "seconds": t,
+            "math": CPU_MATH}
 
 
 def oracle_simulate():
     from oracle import pyoracle
 
     def simulate(name, flat, n_groups, n_particles, dt, seed, times):
-        import dust2_gb300 as d
-        rng = np.frombuffer(d.rng_streams(n_groups * n_particles, seed),
-                            dtype="<u8")
+        rng = pyoracle.rng_streams(n_groups * n_particles, seed)
         out, _ = pyoracle.port().discrete_simulate(
             name, flat, n_groups, n_particles, 0.0, dt, rng, times)
         n_state = N_STATE[name]

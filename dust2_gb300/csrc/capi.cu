@@ -1002,6 +1002,15 @@ int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
   });
 }
 
+int dust2_gb300_filter_reorder_times(dust2_gb300_filter* filter,
+                                     double* ms, int64_t* n_launches) {
+  return guard([&] {
+    long n = 0;
+    filref(filter).reorder_times(ms, &n);
+    *n_launches = n;
+  });
+}
+
 int dust2_gb300_unfilter_alloc(const char* name, const double* pars,
                                size_t n_groups, size_t n_particles,
                                double time_start, const double* time,

@@ -144,6 +144,9 @@ public:
   virtual void set_timing(bool enable) = 0;
   virtual void kernel_times(double* step_ms, long* n_step_launches,
                             double* run_ms, long* n_runs) = 0;
+  // Device time of the reorder (state gather) launches timed the same
+  // way, when the tail runs as separate kernels (else none are timed).
+  virtual void reorder_times(double* ms, long* n_launches) = 0;
   // Save trajectories in the following runs (index_state: state entries,
   // nullptr = all); export those of the last run for `groups`, all
   // particles or select[i] of each, as [time][group][particle][state].

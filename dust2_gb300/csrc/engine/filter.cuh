@@ -146,13 +146,24 @@ __device__ __forceinline__ void step_compare_tile(
     const int k = tl.start + threadIdx.x;
     auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
     typename T::internal_state internal{};
-    double x[T::n_state_max];
-    double y[T::n_state_max];
-    load_state<T>(v, k, x);
-    run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
-                    sm.zero_steps, rng, x, y);
-    logw = T::compare_data(time_compare, x, *d, sm.shared(), internal, rng);
-    store_state<T>(v, k, x);
+    if constexpr (smem_state<T>::enabled) {
+      double* x = state_row<T>();
+      load_state<T>(v, k, x);
+      run_particle_in_place<T>(time, dt, n_steps, sm.shared(), internal,
+                               sm.zero, sm.zero_steps, rng, x);
+      logw = T::compare_data(time_compare, x, *d, sm.shared(), internal,
+                             rng);
+      store_state<T>(v, k, x);
+    } else {
+      double x[T::n_state_max];
+      double y[T::n_state_max];
+      load_state<T>(v, k, x);
+      run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
+                      sm.zero_steps, rng, x, y);
+      logw = T::compare_data(time_compare, x, *d, sm.shared(), internal,
+                             rng);
+      store_state<T>(v, k, x);
+    }
     store_rng(v.rng, v.stride, k, rng);
     capture_error(v.errors, v.any_error, k, rng);
     f.w[k] = logw;
@@ -391,6 +402,9 @@ public:
                                data.size() * sizeof(data_type),
                                cudaMemcpyHostToDevice, s));
     put_rng_state(rng_words.data());
+    if constexpr (!is_continuous<T>()) {
+      smem_state<T>::allow(k_step_compare<T>, default_tile_size<T>());
+    }
     sys_->sync();
     set_fused_tail(true);
     // k_group: one warp per window of 32 chunks of the largest group
@@ -669,8 +683,18 @@ public:
     }
     step_ms_ = 0;
     run_ms_ = 0;
+    reorder_ms_ = 0;
     n_step_launches_ = 0;
+    n_reorder_launches_ = 0;
     n_timed_runs_ = 0;
+  }
+
+  void reorder_times(double* ms, long* n_launches) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    *ms = reorder_ms_;
+    *n_launches = n_reorder_launches_;
   }
 
   void kernel_times(double* step_ms, long* n_step_launches, double* run_ms,
@@ -845,6 +869,9 @@ public:
     for (auto e : ev_run_) {
       cudaEventDestroy(e);
     }
+    for (auto e : ev_reorder_) {
+      cudaEventDestroy(e);
+    }
     if (graph_exec_ != nullptr) {
       cudaGraphExecDestroy(graph_exec_);
     }
@@ -888,8 +915,12 @@ private:
           st.t_compare, owner_->dt(), i == 0 ? 1 : 0,
           data_.data() + i * n_groups_data_, n_groups_data_);
       } else {
-        k_step_compare<T><<<NT, TS, 0, s>>>(
-          v, f, st.t0, S.dt(), st.n_steps, st.t_compare,
+        system_view<T> vs = v;
+        vs.tiles = S.step_tiles_dev();
+        const int step_block = S.step_block();
+        k_step_compare<T><<<S.n_step_tiles(), step_block,
+                            smem_state<T>::bytes(step_block), s>>>(
+          vs, f, st.t0, S.dt(), st.n_steps, st.t_compare,
           data_.data() + i * n_groups_data_, n_groups_data_);
       }
       if (timing_) {
@@ -903,10 +934,16 @@ private:
         k_group<<<G, group_threads_, 0, s>>>(f, G);
         k_resample<<<NT, TS, 0, s>>>(f);
         k_fallback_counted(f, s);
+        if (timing_) {
+          record(ev_reorder_[2 * i]);
+        }
         k_reorder<<<NT, TS, 0, s>>>(cur, other, L.stride, S.n_state(),
                                     L.tiles.empty() ? nullptr :
                                     S.tiles_dev(), offset_.data(),
                                     idx_.data(), mode_.data());
+        if (timing_) {
+          record(ev_reorder_[2 * i + 1]);
+        }
       }
       if constexpr (is_continuous<T>()) {
         owner_->enqueue_reorder_record(S.tiles_dev(), NT, TS, offset_.data(),
@@ -950,6 +987,11 @@ private:
       DUST2_CUDA(cudaEventCreate(&e));
       ev_step_.push_back(e);
     }
+    while (ev_reorder_.size() < need) {
+      cudaEvent_t e;
+      DUST2_CUDA(cudaEventCreate(&e));
+      ev_reorder_.push_back(e);
+    }
     while (ev_run_.size() < 2) {
       cudaEvent_t e;
       DUST2_CUDA(cudaEventCreate(&e));
@@ -970,6 +1012,12 @@ private:
                                       ev_step_[2 * i + 1]));
       step_ms_ += ms;
       n_step_launches_++;
+      if (!fused_tail_) {
+        DUST2_CUDA(cudaEventElapsedTime(&ms, ev_reorder_[2 * i],
+                                        ev_reorder_[2 * i + 1]));
+        reorder_ms_ += ms;
+        n_reorder_launches_++;
+      }
     }
     float ms = 0;
     DUST2_CUDA(cudaEventElapsedTime(&ms, ev_run_[0], ev_run_[1]));
@@ -1046,9 +1094,12 @@ private:
   std::vector<int> fallback_host_;
   std::vector<cudaEvent_t> ev_step_;
   std::vector<cudaEvent_t> ev_run_;
+  std::vector<cudaEvent_t> ev_reorder_;
   double step_ms_ = 0;
   double run_ms_ = 0;
+  double reorder_ms_ = 0;
   long n_step_launches_ = 0;
+  long n_reorder_launches_ = 0;
   long n_timed_runs_ = 0;
 
   device_array<int> active_, n_part_, offset_, chunk_first_, chunk_count_;

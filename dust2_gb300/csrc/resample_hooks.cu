@@ -91,17 +91,17 @@ std::size_t hook_scratch_bytes(std::size_t n, int tile_size) {
 
 // Lay the hook's arrays out in one device region (256-byte aligned
 // pieces) and fill the per-group scalars and tiles.  `base` must hold
-// hook_scratch_bytes(n) bytes.
-void hook_layout(char* base, std::size_t n, int tile_size,
-                 const std::vector<tile>& tiles, hook_buffers& hb,
-                 cudaStream_t s) {
+// hook_scratch_bytes(n) bytes.  Every per-group scalar is rewritten, so
+// nothing an earlier call left in the same memory is read.
+void hook_layout(char* base, std::size_t n, const tile* tiles, int n_tiles,
+                 hook_buffers& hb, cudaStream_t s) {
   std::size_t off = 0;
   auto take = [&](std::size_t bytes) {
     char* p = base + off;
     off += (bytes + 255) / 256 * 256;
     return p;
   };
-  const std::size_t nt = tiles.size();
+  const std::size_t nt = static_cast<std::size_t>(n_tiles);
   filter_view& f = hb.f;
   f.w = reinterpret_cast<double*>(take(n * 8));
   f.ew = reinterpret_cast<double*>(take(n * 8));
@@ -137,9 +137,9 @@ void hook_layout(char* base, std::size_t n, int tile_size,
                              cudaMemcpyHostToDevice, s));
   const unsigned long long key0 = 0;  // below every ordered key
   DUST2_CUDA(cudaMemcpyAsync(f.gkey, &key0, 8, cudaMemcpyHostToDevice, s));
-  DUST2_CUDA(cudaMemcpyAsync(t_dev, tiles.data(), nt * sizeof(tile),
+  DUST2_CUDA(cudaMemcpyAsync(t_dev, tiles, nt * sizeof(tile),
                              cudaMemcpyHostToDevice, s));
-  hb.n_tiles = static_cast<int>(nt);
+  hb.n_tiles = n_tiles;
 }
 
 // Systematic resampling of raw weights already in hb.f.w; indices left
@@ -184,7 +184,8 @@ int dust2_gb300_resample_weight(const double* w, size_t n, double u,
     cudaStream_t s;
     DUST2_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     hook_buffers hb;
-    hook_layout(scratch.data(), n, HOOK_TILE, tiles, hb, s);
+    hook_layout(scratch.data(), n, tiles.data(),
+                static_cast<int>(tiles.size()), hb, s);
     DUST2_CUDA(cudaMemsetAsync(count.data(), 0, sizeof(int), s));
     DUST2_CUDA(cudaMemcpyAsync(hb.f.w, w, n * 8, cudaMemcpyHostToDevice, s));
     hook_resample(hb, u, HOOK_TILE, 0, count.data(), s);
@@ -218,7 +219,8 @@ int dust2_gb300_scale_log_weights(double* w, size_t n, double* result) {
     cudaStream_t s;
     DUST2_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     hook_buffers hb;
-    hook_layout(scratch.data(), n, HOOK_TILE, tiles, hb, s);
+    hook_layout(scratch.data(), n, tiles.data(),
+                static_cast<int>(tiles.size()), hb, s);
     DUST2_CUDA(cudaMemcpyAsync(hb.f.w, w, n * 8, cudaMemcpyHostToDevice, s));
     k_reduce_log_weights<<<hb.n_tiles, HOOK_TILE, 0, s>>>(hb.f);
     unsigned long long key = 0;

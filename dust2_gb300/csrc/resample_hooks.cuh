@@ -22,16 +22,10 @@ struct hook_buffers {
 std::size_t hook_scratch_bytes(std::size_t n, int tile_size);
 
 // Lay the arrays out in `base` (hook_scratch_bytes(n) bytes, 256-byte
-// aligned) and fill the per-group scalars and tiles.
-void hook_layout(char* base, std::size_t n, int tile_size,
-                 const std::vector<tile>& tiles, hook_buffers& hb,
-                 cudaStream_t s);
-
-// As hook_layout, with the tiles given as a plain array (no container),
-// for the entry point that must not allocate.
-void hook_layout_fixed(char* base, std::size_t n, int tile_size,
-                       const tile* tiles, int n_tiles, hook_buffers& hb,
-                       cudaStream_t s);
+// aligned) and fill the per-group scalars and the n_tiles tiles (a host
+// array; nothing is allocated on the host or the device).
+void hook_layout(char* base, std::size_t n, const tile* tiles, int n_tiles,
+                 hook_buffers& hb, cudaStream_t s);
 
 // Systematic resampling of the raw weights in hb.f.w with uniform u;
 // indices (group-local) are left in hb.f.idx.

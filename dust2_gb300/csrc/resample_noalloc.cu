@@ -11,15 +11,22 @@
 // onto a device and kept until the process exits.
 //
 // Limits and sharing:
-//   * at most NOALLOC_MAX_N = 65536 weights per call (about 1.9 MB of
-//     scratch, held by every device that loads this library);
+//   * the array takes 2 MiB on every device that loads this library; a
+//     call uses at most about 1.9 MB of it (NOALLOC_MAX_N = 65536
+//     weights per call);
 //   * every call uses the same array, which keeps the previous call's
 //     contents; everything that must start at zero is cleared per call;
 //   * calls that overlap on the GPU race on that array (for example, two
 //     host threads calling at once): serialise them;
+//   * the work runs on the calling thread's per-thread default stream
+//     (cudaStreamPerThread), which needs nothing created and does not
+//     wait for the caller's other streams;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first
-//     call before any stream capture on the device.
+//     (cudaGetSymbolAddress) with that device current, and later calls
+//     reuse it; make that first call before any stream capture on the
+//     device, and do not call the entry point on a device after
+//     cudaDeviceReset in the same process (the library's module may then
+//     be loaded at another address).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -113,11 +120,12 @@ extern "C" int dust2_gb300_resample_weight_noalloc(const double* w, size_t n,
       throw std::runtime_error("resampling scratch array too small");
     }
     char* base = scratch_on_current_device();
-    const cudaStream_t s = 0;  // the legacy default stream: nothing created
+    // the calling thread's default stream: nothing is created, and it
+    // does not wait for the caller's other (blocking) streams
+    const cudaStream_t s = cudaStreamPerThread;
     int* fallback_count = reinterpret_cast<int*>(base);
     hook_buffers hb;
-    hook_layout_fixed(base + 256, n, NOALLOC_TILE, tiles, nt, hb, s);
-    (void)NOALLOC_MAX_TILES;
+    hook_layout(base + 256, n, tiles, nt, hb, s);
     DUST2_CUDA(cudaMemsetAsync(fallback_count, 0, sizeof(int), s));
     DUST2_CUDA(cudaMemcpyAsync(hb.f.w, w, n * sizeof(double),
                                cudaMemcpyHostToDevice, s));

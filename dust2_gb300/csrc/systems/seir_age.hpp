@@ -18,9 +18,13 @@ namespace systems {
 
 struct seir_age {
   static constexpr const char* name = "seir_age";
-  // kernels of this system fit 3 blocks of 128 threads per SM (170
-  // registers): measured 2.6% faster than 2 blocks (255 registers)
-  static constexpr int min_blocks_per_sm = 3;
+  // update() reads the entries of age a (and, before its loop, every I)
+  // before it writes the same entries of state_next, and reads nothing
+  // it has written: it is correct in place, so the step kernels keep
+  // each particle's 96 doubles in a row of shared memory.  Two blocks of
+  // 128 such rows (99 KB each) fill an SM.
+  static constexpr bool update_in_place = true;
+  static constexpr int min_blocks_per_sm = 2;
   using real_type = double;
   using rng_state_type = random::rng_state;
   static constexpr int n_age = 16;

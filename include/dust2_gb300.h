@@ -350,14 +350,17 @@ int dust2_gb300_scale_log_weights(double* w, size_t n, double* result);
 
 /* dust2_gb300_resample_weight without any device allocation: the
  * working arrays live in a fixed scratch area compiled into the library
- * (about 1.9 MB, held by every device that loads it).  For callers that
- * cannot allocate device memory at call time, e.g. when another allocator
- * owns the GPU's memory or when cudaFree's device-wide synchronisation is
- * unacceptable.  At most 65536 weights (an error otherwise).  The first
- * call on a device looks up the scratch area's address with that device
- * current: make it before any stream capture.  All calls share the area,
- * so calls that overlap on the GPU race: serialise them.  No counterpart
- * in dust2. */
+ * (2 MiB reserved on every device that loads it; a call uses at most
+ * about 1.9 MB).  For callers that cannot allocate device memory at call
+ * time, e.g. when another allocator owns the GPU's memory or when
+ * cudaFree's device-wide synchronisation is unacceptable.  At most 65536
+ * weights (an error otherwise).  Runs on the calling thread's per-thread
+ * default stream (cudaStreamPerThread).  The first call on a device looks
+ * up the scratch area's address with that device current and later calls
+ * reuse it: make the first call before any stream capture, and do not
+ * call it on a device after cudaDeviceReset in the same process.  All
+ * calls share the area, so calls that overlap on the GPU race: serialise
+ * them.  No counterpart in dust2. */
 int dust2_gb300_resample_weight_noalloc(const double* w, size_t n, double u,
                                         size_t* idx);
 
@@ -402,6 +405,14 @@ int dust2_gb300_filter_set_timing(dust2_gb300_filter* filter, int32_t enable);
 int dust2_gb300_filter_kernel_times(dust2_gb300_filter* filter,
                                     double* step_ms, int64_t* n_step_launches,
                                     double* run_ms, int64_t* n_runs);
+
+/* Accumulated device time (ms) and number of the reorder launches (the
+ * state gather of discrete/system.hpp:170-181) timed the same way; none
+ * are timed when the filter's tail runs as one cluster launch (groups of
+ * at most 1024 particles).  No counterpart in the reference: it serves
+ * the benchmark's HBM roofline of the gather. */
+int dust2_gb300_filter_reorder_times(dust2_gb300_filter* filter, double* ms,
+                                     int64_t* n_launches);
 
 /* ---- deterministic likelihood (r/unfilter.hpp, unfilter.hpp) ---------- */
 

@@ -21,8 +21,13 @@ PORT_SRC = HERE / "port" / "oracle.cpp"
 PORT_LIB = HERE / "_build" / "liboracle.so"
 PORT_LIBM_LIB = HERE / "_build" / "liboracle_libm.so"
 REF_LIB = HERE / "_ref" / "libdust2_ref.so"
-REF_INCLUDE = Path(os.environ.get("DUST2_REF",
-                                  "/root/reference/inst/include"))
+
+
+def ref_include(path=None):
+    """The reference's inst/include directory: the argument, else the
+    DUST2_REF environment variable; None when neither is given."""
+    path = path or os.environ.get("DUST2_REF")
+    return Path(path) if path else None
 
 
 def _inputs():
@@ -54,13 +59,17 @@ def build_port(force=False, libm=False):
     return lib
 
 
-def build_ref(force=False):
-    """Build the reference-engine oracle; None when sources are absent."""
-    if not (REF_INCLUDE / "dust2" / "filter.hpp").exists():
+def build_ref(force=False, include=None):
+    """Build the reference-engine oracle from the reference's
+    inst/include directory (`include`, else $DUST2_REF); None when the
+    sources are not there."""
+    inc = ref_include(include)
+    if inc is None or not (inc / "dust2" / "filter.hpp").exists():
         return None
-    cmd = ["make", "-s", "-C", str(HERE), f"REF={REF_INCLUDE}"]
+    cmd = ["make", "-s", "-C", str(HERE), f"REF={inc}"]
     if force:
-        subprocess.run(["make", "-s", "-C", str(HERE), "clean"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), f"REF={inc}",
+                        "clean"], check=True)
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"reference build failed:\n{res.stdout}\n"

@@ -1485,4 +1485,39 @@ void oracle_resample_weight(int n, const double* w, double u, int64_t* idx) {
   }
 }
 
+// The parameter table of a discrete-time system as text, one
+// "name length" pair per line (so that callers can pack parameter rows
+// without the CUDA library).  Returns the text length, or -1 for an
+// unknown system or a buffer that is too small.
+int oracle_parameters(const char* name, char* out, int len) {
+  std::string text;
+  const bool ok = dispatch_discrete(name, [&](auto t) {
+    using S = typename decltype(t)::type;
+    for (const auto& p : S::parameters) {
+      text += std::string(p.name) + " " + std::to_string(p.length) + "\n";
+    }
+  });
+  if (!ok || static_cast<int>(text.size()) >= len) {
+    return -1;
+  }
+  std::memcpy(out, text.c_str(), text.size() + 1);
+  return static_cast<int>(text.size());
+}
+
+// The first n streams of an integer seed: SplitMix64 expansion of the
+// seed into the first stream, then one 2^128 jump per further stream
+// (the stream contract of dust2's filters, r/discrete/filter.hpp:63-75).
+void oracle_rng_streams(uint64_t seed, int n, uint64_t* out) {
+  uint64_t s[4];
+  dust2gpu::random::seed_state(seed, s);
+  for (int k = 0; k < n; ++k) {
+    if (k > 0) {
+      dust2gpu::random::jump(s);
+    }
+    for (int w = 0; w < 4; ++w) {
+      out[4 * static_cast<size_t>(k) + w] = s[w];
+    }
+  }
+}
+
 }  // extern "C"

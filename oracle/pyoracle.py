@@ -471,3 +471,37 @@ def port_density(dist, x, a, b=0.0):
     f(ctypes.c_int(code), x.ctypes.data_as(_d), ctypes.c_int(x.size),
       ctypes.c_double(a), ctypes.c_double(b), out.ctypes.data_as(_d))
     return out
+
+
+def rng_streams(n_streams, seed):
+    """Words (uint64) of the first n_streams streams of an integer seed,
+    computed by the oracle (no CUDA library involved)."""
+    o = port()
+    out = np.empty(4 * n_streams, dtype=np.uint64)
+    f = o.lib.oracle_rng_streams
+    f.restype = None
+    f(ctypes.c_uint64(int(seed) % (1 << 64)), ctypes.c_int(n_streams),
+      out.ctypes.data_as(_u))
+    return out
+
+
+def pack_pars(name, pars):
+    """A flat parameter row (NaN where not given) of a discrete-time
+    system from a dict, laid out by the system's parameter table as the
+    oracle reads it (no CUDA library involved)."""
+    o = port()
+    buf = ctypes.create_string_buffer(1 << 14)
+    f = o.lib.oracle_parameters
+    f.restype = ctypes.c_int
+    if f(name.encode(), buf, len(buf)) < 0:
+        raise OracleError(f"unknown system {name}")
+    table = [(ln.split()[0], int(ln.split()[1]))
+             for ln in buf.value.decode().splitlines()]
+    row = np.full(sum(n for _, n in table), np.nan)
+    off = 0
+    for nm, n in table:
+        if nm in pars and pars[nm] is not None:
+            v = np.asarray(pars[nm], dtype=np.float64).ravel()
+            row[off:off + v.size] = v
+        off += n
+    return row

@@ -6,7 +6,10 @@ dust2_gb300_resample_weight_noalloc, which works in a scratch area
 compiled into the library.  Its indices must be identical to those of
 dust2_gb300_resample_weight (the allocating entry point running the same
 kernels) -- resampling indices are integer results, compared exactly -- on
-consecutive calls that reuse the shared scratch area.
+consecutive calls that reuse the shared scratch area -- and equal to the
+CPU oracle's serial algorithm on weights whose decisions sit within
+rounding distance of a boundary, where the exact serial fallback runs
+inside the scratch area too.
 
 This file is collected last so that a failure here leaves every other
 test already run; it also passes on its own in a fresh process."""
@@ -56,3 +59,52 @@ def test_no_alloc_rejects_sizes_above_its_limit(lib_ready):
     from dust2_gb300 import _lib
     with pytest.raises(_lib.DustError, match="above the limit of 65536"):
         _call("dust2_gb300_resample_weight_noalloc", np.ones(65537), 0.5)
+
+
+def test_no_alloc_near_ties_match_oracle(lib_ready):
+    # weights that make the parallel decision ambiguous (equal weights,
+    # powers of two down to subnormals, halfway sums, sparse weights, 700
+    # orders of magnitude), so that the exact serial fallback runs in the
+    # fixed scratch area; compared with the oracle directly, two calls in
+    # a row each
+    from oracle import pyoracle
+    port = pyoracle.port()
+    rs = np.random.default_rng(23)
+    n = 40000
+    cases = [np.ones(n), np.ldexp(1.0, -rs.integers(0, 1100, n)),
+             rs.integers(0, 4, n) * 0.5,
+             np.where(rs.uniform(size=n) < 0.95, 0.0, rs.uniform(size=n)),
+             np.exp(-700 * rs.uniform(size=n))]
+    for w in cases:
+        for u in (0.0, 0.5, 1 - 1e-12):
+            want = port.resample_weight(w, u)
+            for _ in range(2):
+                got = _call("dust2_gb300_resample_weight_noalloc", w, u)
+                np.testing.assert_array_equal(got, want)
+
+
+def test_no_alloc_first_call_on_a_second_device(lib_ready):
+    # the scratch address is looked up per device on its first call: a
+    # first call on device 1 after calls on device 0 must use device 1's
+    # own array (boxes with one GPU skip this)
+    import dust2_gb300 as d
+    if d.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    rs = np.random.default_rng(4)
+    w = np.abs(rs.standard_cauchy(5000))
+    expect = _call("dust2_gb300_resample_weight", w, 0.25)
+    # the CUDA runtime the library is linked against (already loaded, so
+    # this is the same instance and its current device is the library's)
+    cudart = ctypes.CDLL("libcudart.so.13")
+    np.testing.assert_array_equal(
+        _call("dust2_gb300_resample_weight_noalloc", w, 0.25), expect)
+    prev = ctypes.c_int()
+    assert cudart.cudaGetDevice(ctypes.byref(prev)) == 0
+    try:
+        assert cudart.cudaSetDevice(1) == 0
+        np.testing.assert_array_equal(
+            _call("dust2_gb300_resample_weight", w, 0.25), expect)
+        np.testing.assert_array_equal(
+            _call("dust2_gb300_resample_weight_noalloc", w, 0.25), expect)
+    finally:
+        cudart.cudaSetDevice(prev.value)
