@@ -19,7 +19,7 @@ from .interface import (
     dust_system_update_pars, dust_unfilter_create, dust_unpack_index,
     dust_unpack_state, logistic, malaria,
     resample_weight, rng_streams,
-    scale_log_weights, seir_age, sir, sir_cases, sirode, walk)
+    scale_log_weights, seir_age, sir, sir_cases, sirode, sirs, walk)
 
 __all__ = [
     "DustError", "DustLikelihood", "DustServer", "DustSystem",
@@ -41,4 +41,4 @@ __all__ = [
     "dust_unpack_index", "dust_unpack_state",
     "logistic", "malaria",
     "resample_weight", "rng_streams", "scale_log_weights", "seir_age", "sir",
-    "sir_cases", "sirode", "walk"]
+    "sir_cases", "sirode", "sirs", "walk"]

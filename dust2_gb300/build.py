@@ -27,7 +27,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
     "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-strict-aliasing",
-    "-I", str(CSRC), "-I", str(REPO / "include"),
+    "-I", str(CSRC), "-I", str(CSRC / "compat"), "-I", str(REPO / "include"),
 ]
 
 

@@ -215,6 +215,26 @@ constexpr int n_special() {
   }
 }
 
+// One data row of a system: `build_data(row)`, or `build_data(row,
+// shared)` for systems that read the group's shared state (dust2's
+// build_data takes it, e.g. for dimensions: inst/examples/sir.cpp).
+template <class T, class = void>
+struct build_data_takes_shared : std::false_type {};
+template <class T>
+struct build_data_takes_shared<T, std::void_t<decltype(T::build_data(
+  std::declval<const double*>(),
+  std::declval<const typename T::shared_state&>()))>> : std::true_type {};
+
+template <typename T>
+typename T::data_type build_data_of(const double* row,
+                                    const typename T::shared_state& shared) {
+  if constexpr (build_data_takes_shared<T>::value) {
+    return T::build_data(row, shared);
+  } else {
+    return T::build_data(row);
+  }
+}
+
 // Static checks every system must pass before the engine accepts it.
 template <typename T>
 constexpr bool check_system() {

@@ -148,12 +148,43 @@ __device__ __forceinline__ void apply_zero_every(
   }
 }
 
+// States updated in place, and large states in shared memory.
+//
+// A system may declare `static constexpr bool update_in_place = true`
+// when its `update` is correct with `state_next == state`: it reads each
+// state entry before it writes that entry of state_next and never reads
+// an entry after writing it.  Its particles then keep one state array
+// instead of two.
+//
+// Such a system may also declare `static constexpr bool
+// state_in_shared_memory = true`: the filter's step kernel and k_run then
+// keep each particle's state in one row of dynamic shared memory rather
+// than in a per-thread array (which, for a state too large for registers,
+// lives in local memory).  Rows have an odd pitch (in doubles), so the 16
+// threads of a half-warp that access the same entry of their rows hit 16
+// different bank pairs.  This trades occupancy for local-memory traffic:
+// a 96-double row per thread allows 8 warps per SM.  The arithmetic, and
+// so every result, is the same on every path.
+template <typename T, typename = void>
+struct update_in_place_of : std::false_type {};
+template <typename T>
+struct update_in_place_of<T, std::void_t<decltype(T::update_in_place)>>
+  : std::integral_constant<bool, T::update_in_place> {};
+
+template <typename T, typename = void>
+struct state_in_smem_of : std::false_type {};
+template <typename T>
+struct state_in_smem_of<T,
+                        std::void_t<decltype(T::state_in_shared_memory)>>
+  : std::integral_constant<bool, T::state_in_shared_memory> {};
+
 // Advance one particle n_steps; on return the state is in x.  The
 // reference swaps the two state pointers after each step; since `update`
 // writes every entry of `state_next`, copying y back into x (register
 // moves) is equivalent and keeps a single inlined copy of `update` in the
 // loop (the samplers make it large; instruction-cache misses showed up as
-// "no instruction" stalls when the loop held three copies).
+// "no instruction" stalls when the loop held three copies).  A system
+// updated in place steps x itself (y is unused).
 template <typename T>
 __device__ __forceinline__ void run_particle(
     double time, double dt, int n_steps,
@@ -164,40 +195,23 @@ __device__ __forceinline__ void run_particle(
   for (int i = 0; i < n_steps; ++i) {
     const double t = time + static_cast<double>(i) * dt;
     apply_zero_every<T>(z, zero_steps, i, t, x);
-    T::update(t, dt, x, shared, internal, rng, y);
+    if constexpr (update_in_place_of<T>::value) {
+      T::update(t, dt, x, shared, internal, rng, x);
+    } else {
+      T::update(t, dt, x, shared, internal, rng, y);
 #pragma unroll
-    for (int s = 0; s < T::n_state_max; ++s) {
-      x[s] = y[s];
+      for (int s = 0; s < T::n_state_max; ++s) {
+        x[s] = y[s];
+      }
     }
   }
 }
 
-// Large states in shared memory.
-//
-// A state of more than 32 doubles does not fit in registers beside the
-// samplers' working set.  As a per-thread array it lives in local memory,
-// and with two such arrays (state and state_next) per particle a block of
-// 128 SEIR particles (96 doubles each) needs 192 KB: far more than L1, so
-// every step moved kilobytes per particle through L2 and HBM.
-//
-// A system may declare `static constexpr bool update_in_place = true`
-// when its `update` is correct with `state_next == state`: it reads each
-// state entry before it writes that entry of state_next and never reads
-// an entry after writing it.  The step kernels then keep each particle's
-// state in one row of dynamic shared memory and step it in place.  Rows
-// have an odd pitch (in doubles), so the 16 threads of a half-warp that
-// access the same entry of their rows hit 16 different bank pairs.  The
-// arithmetic, and so every result, is the same as on the register path.
-template <typename T, typename = void>
-struct update_in_place_of : std::false_type {};
-template <typename T>
-struct update_in_place_of<T, std::void_t<decltype(T::update_in_place)>>
-  : std::integral_constant<bool, T::update_in_place> {};
-
 template <typename T>
 struct smem_state {
   static constexpr bool enabled = T::n_state_max > 32 &&
-    update_in_place_of<T>::value && !is_continuous<T>();
+    update_in_place_of<T>::value && state_in_smem_of<T>::value &&
+    !is_continuous<T>();
   static constexpr int pitch = T::n_state_max | 1;
   // dynamic shared memory of a block of `threads` particles
   static std::size_t bytes(int threads) {
@@ -806,7 +820,8 @@ public:
       const int nd = n_data();
       std::vector<data_type> d;
       for (int g = 0; g < n_groups_data; ++g) {
-        d.push_back(T::build_data(data + static_cast<std::size_t>(g) * nd));
+        d.push_back(build_data_of<T>(data + static_cast<std::size_t>(g) * nd,
+                                     shared_[n_groups_data == 1 ? 0 : g]));
       }
       device_array<data_type> d_dev(d.size());
       device_array<double> o(layout_.n_total);

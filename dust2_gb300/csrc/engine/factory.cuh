@@ -102,6 +102,15 @@ filter_api* create_filter(const double* pars, int n_groups,
   } else {
     bind_lf_table();
     auto shared = build_shared_groups<T>(pars, n_groups);
+    // data rows, [time][group] (one group's row when data are shared)
+    const int nd = static_cast<int>(sizeof(typename T::data_type) /
+                                    sizeof(double));
+    std::vector<typename T::data_type> d;
+    d.reserve(static_cast<std::size_t>(n_times) * n_groups_data);
+    for (int i = 0; i < n_times * n_groups_data; ++i) {
+      d.push_back(build_data_of<T>(data + static_cast<std::size_t>(i) * nd,
+                                   shared[i % n_groups_data]));
+    }
     // Split the stream block (r/discrete/filter.hpp:63-75): per group the
     // first 2 streams go to the filter, the rest to the particles.
     std::vector<std::uint64_t> sys_words;
@@ -115,12 +124,6 @@ filter_api* create_filter(const double* pars, int n_groups,
     auto sys = make_filter_system<T>(std::move(shared), time_start, dt,
                                      control, n_particles, sys_words,
                                      tile_size);
-    const int nd = sys->n_data();
-    std::vector<typename T::data_type> d;
-    d.reserve(static_cast<std::size_t>(n_times) * n_groups_data);
-    for (int i = 0; i < n_times * n_groups_data; ++i) {
-      d.push_back(T::build_data(data + static_cast<std::size_t>(i) * nd));
-    }
     std::vector<double> t(times, times + n_times);
     return new filter_engine<T>(std::move(sys), time_start, std::move(t),
                                 std::move(d), n_groups_data, rng_words);
@@ -164,7 +167,8 @@ unfilter_api* create_unfilter(const double* pars, int n_groups,
     const int nd = static_cast<int>(sizeof(typename T::data_type) /
                                     sizeof(double));
     for (int i = 0; i < n_times * n_groups_data; ++i) {
-      d.push_back(T::build_data(data + static_cast<std::size_t>(i) * nd));
+      d.push_back(build_data_of<T>(data + static_cast<std::size_t>(i) * nd,
+                                   shared[i % n_groups_data]));
     }
     std::vector<double> t(times, times + n_times);
     if constexpr (is_continuous<T>()) {

@@ -460,8 +460,8 @@ public:
     }
     const int nd = n_data();
     for (int i = 0; i < n_times; ++i) {
-      ss->data.push_back(T::build_data(data + static_cast<std::size_t>(i) *
-                                       nd));
+      ss->data.push_back(build_data_of<T>(
+        data + static_cast<std::size_t>(i) * nd, ss->shared));
     }
     ss->rng_words = std::move(rng_words);
     std::lock_guard<std::mutex> lock(mu_);

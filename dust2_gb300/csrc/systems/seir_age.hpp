@@ -20,10 +20,12 @@ struct seir_age {
   static constexpr const char* name = "seir_age";
   // update() reads the entries of age a (and, before its loop, every I)
   // before it writes the same entries of state_next, and reads nothing
-  // it has written: it is correct in place, so the step kernels keep
-  // each particle's 96 doubles in a row of shared memory.  Two blocks of
-  // 128 such rows (99 KB each) fill an SM.
+  // it has written: it is correct in place, so a particle keeps one
+  // state array.
   static constexpr bool update_in_place = true;
+  // the step kernels keep each particle's 96 doubles in a row of shared
+  // memory; two blocks of 128 such rows (99 KB each) fill an SM
+  static constexpr bool state_in_shared_memory = true;
   static constexpr int min_blocks_per_sm = 2;
   using real_type = double;
   using rng_state_type = random::rng_state;

@@ -103,6 +103,11 @@ def seir_age():
     return Generator("seir_age")
 
 
+def sirs():
+    """SIRS written as a dust2 class (the compat plugin adapter)."""
+    return Generator("sirs")
+
+
 def _generator(generator):
     if isinstance(generator, Generator):
         return generator

@@ -33,6 +33,7 @@ def ref_include(path=None):
 def _inputs():
     return ([PORT_SRC] + list((CSRC / "dust2gpu").glob("*.hpp")) +
             list((CSRC / "systems").glob("*.hpp")) +
+            list((CSRC / "compat").rglob("*.hpp")) +
             [CSRC / "engine" / "error_text.hpp", Path(__file__)])
 
 
@@ -48,7 +49,8 @@ def build_port(force=False, libm=False):
     lib.parent.mkdir(exist_ok=True)
     tmp = lib.with_suffix(".so.tmp")
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-fPIC", "-shared",
-           "-ffp-contract=off", "-fno-strict-aliasing", "-I", str(CSRC)]
+           "-ffp-contract=off", "-fno-strict-aliasing", "-I", str(CSRC),
+           "-I", str(CSRC / "compat")]
     if libm:
         cmd.append("-DDUST2_HOST_LIBM")
     cmd += [str(PORT_SRC), "-o", str(tmp)]

@@ -34,6 +34,7 @@
 #include "systems/sir.hpp"
 #include "systems/sir_cases.hpp"
 #include "systems/sirode.hpp"
+#include "systems/sirs.hpp"
 #include "systems/walk.hpp"
 
 namespace {
@@ -57,6 +58,8 @@ bool dispatch_discrete(const std::string& name, F f) {
     f(tag<walk>{});
   } else if (name == "seir_age") {
     f(tag<seir_age>{});
+  } else if (name == "sirs") {
+    f(tag<dust2gpu::systems::sirs>{});
   } else {
     return false;
   }
@@ -354,7 +357,8 @@ struct filter_port {
     n_groups_data(n_groups_data_) {
     const int nd = sizeof(typename S::data_type) / sizeof(double);
     for (int i = 0; i < n_times * n_groups_data; ++i) {
-      data.push_back(S::build_data(d + static_cast<size_t>(i) * nd));
+      data.push_back(dust2gpu::build_data_of<S>(
+        d + static_cast<size_t>(i) * nd, sys.shared[i % n_groups_data]));
     }
     size_t pos = 0;
     for (int n : np) {
@@ -961,7 +965,8 @@ int oracle_compare(const char* name, const double* pars, int n_groups,
         std::vector<typename S::data_type> d;
         const int nd = sizeof(typename S::data_type) / sizeof(double);
         for (int g = 0; g < n_groups_data; ++g) {
-          d.push_back(S::build_data(data + g * nd));
+          d.push_back(dust2gpu::build_data_of<S>(
+            data + g * nd, sys.shared[n_groups_data == 1 ? 0 : g]));
         }
         const std::vector<char> all(n_groups, 1);
         sys.compare_data(d.data(), n_groups_data, all, out);
@@ -1078,7 +1083,8 @@ int oracle_unfilter_adjoint(const char* name, const double* pars,
     const double time_end = time_start + n_steps * dt;
     std::vector<typename S::data_type> d;
     for (int i = 0; i < n_times * n_groups_data; ++i) {
-      d.push_back(S::build_data(data + i));
+      d.push_back(dust2gpu::build_data_of<S>(data + i,
+                                             shared[i % n_groups_data]));
     }
     for (int g = 0; g < n_groups; ++g) {
       const auto z = zero_every_of<S>(shared[g]);
@@ -1184,7 +1190,8 @@ static int unfilter_run_impl(const char* name, const double* pars,
       ctl.step_size_max = step_size_max;
       std::vector<typename S::data_type> d;
       for (int i = 0; i < n_times * n_groups_data; ++i) {
-        d.push_back(S::build_data(data + i));
+        d.push_back(dust2gpu::build_data_of<S>(data + i,
+                                             shared[i % n_groups_data]));
       }
       for (int r = 0; r < n_runs; ++r) {
         errors err_k(n_total);
@@ -1239,7 +1246,9 @@ static int unfilter_run_impl(const char* name, const double* pars,
         std::vector<typename S::data_type> d;
         const int nd = sizeof(typename S::data_type) / sizeof(double);
         for (int i = 0; i < n_times * n_groups_data; ++i) {
-          d.push_back(S::build_data(data + static_cast<size_t>(i) * nd));
+          d.push_back(dust2gpu::build_data_of<S>(
+            data + static_cast<size_t>(i) * nd,
+            sys.shared[i % n_groups_data]));
         }
         const std::vector<char> active(n_groups, 1);
         std::vector<double> step(n_total);
