@@ -148,35 +148,18 @@ __device__ __forceinline__ void apply_zero_every(
   }
 }
 
-// States updated in place, and large states in shared memory.
-//
-// A system may declare `static constexpr bool update_in_place = true`
-// when its `update` is correct with `state_next == state`: it reads each
-// state entry before it writes that entry of state_next and never reads
-// an entry after writing it.  Its particles then keep one state array
-// instead of two.
-//
-// Such a system may also declare `static constexpr bool
-// state_in_shared_memory = true`: the filter's step kernel and k_run then
-// keep each particle's state in one row of dynamic shared memory rather
-// than in a per-thread array (which, for a state too large for registers,
-// lives in local memory).  Rows have an odd pitch (in doubles), so the 16
-// threads of a half-warp that access the same entry of their rows hit 16
-// different bank pairs.  This trades occupancy for local-memory traffic:
-// a 96-double row per thread allows 8 warps per SM.  The arithmetic, and
-// so every result, is the same on every path.
+// States updated in place.  A system may declare `static constexpr bool
+// update_in_place = true` when its `update` is correct with `state_next
+// == state`: it reads each state entry before it writes that entry of
+// state_next and never reads an entry after writing it.  Its particles
+// then keep one state array instead of two, and the copy after each step
+// goes (for a state too large for registers, both arrays live in local
+// memory).  The arithmetic, and so every result, is the same.
 template <typename T, typename = void>
 struct update_in_place_of : std::false_type {};
 template <typename T>
 struct update_in_place_of<T, std::void_t<decltype(T::update_in_place)>>
   : std::integral_constant<bool, T::update_in_place> {};
-
-template <typename T, typename = void>
-struct state_in_smem_of : std::false_type {};
-template <typename T>
-struct state_in_smem_of<T,
-                        std::void_t<decltype(T::state_in_shared_memory)>>
-  : std::integral_constant<bool, T::state_in_shared_memory> {};
 
 // Advance one particle n_steps; on return the state is in x.  The
 // reference swaps the two state pointers after each step; since `update`
@@ -204,77 +187,6 @@ __device__ __forceinline__ void run_particle(
         x[s] = y[s];
       }
     }
-  }
-}
-
-template <typename T>
-struct smem_state {
-  static constexpr bool enabled = T::n_state_max > 32 &&
-    update_in_place_of<T>::value && state_in_smem_of<T>::value &&
-    !is_continuous<T>();
-  static constexpr int pitch = T::n_state_max | 1;
-  // dynamic shared memory of a block of `threads` particles
-  static std::size_t bytes(int threads) {
-    return enabled ?
-      static_cast<std::size_t>(threads) * pitch * sizeof(double) : 0;
-  }
-  // Let `kernel` take bytes(max threads) of dynamic shared memory and
-  // prefer shared memory over L1 (two such blocks fill an SM).
-  template <typename K>
-  static void allow(K kernel, int threads) {
-    if (enabled) {
-      DUST2_CUDA(cudaFuncSetAttribute(
-        kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-        static_cast<int>(bytes(threads))));
-      DUST2_CUDA(cudaFuncSetAttribute(
-        kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-        cudaSharedmemCarveoutMaxShared));
-    }
-  }
-};
-
-// This thread's state row in the block's dynamic shared memory.
-template <typename T>
-__device__ __forceinline__ double* state_row() {
-  extern __shared__ __align__(16) double dust2_state_rows[];
-  return dust2_state_rows + threadIdx.x * smem_state<T>::pitch;
-}
-
-// apply_zero_every for a state held in memory: the masked entries are
-// visited through their set bits rather than by a test of every entry.
-template <typename T>
-__device__ __forceinline__ void apply_zero_every_row(
-    const zero_every_spec& z, const std::uint64_t* zero_steps, int step,
-    double time, double* x) {
-  for (int i = 0; i < z.n; ++i) {
-    const bool hit = (zero_steps != nullptr && step < ZERO_STEPS_CACHED) ?
-      ((zero_steps[i] >> step) & 1) != 0 : fmod(time, z.period[i]) == 0;
-    if (hit) {
-      for (int w = 0; w < ZERO_EVERY_WORDS; ++w) {
-        std::uint64_t m = z.mask[i][w];
-        while (m != 0) {
-          const int s = 64 * w + __ffsll(static_cast<long long>(m)) - 1;
-          if (s < T::n_state_max) {
-            x[s] = 0;
-          }
-          m &= m - 1;
-        }
-      }
-    }
-  }
-}
-
-// run_particle for an update_in_place system whose state is at x.
-template <typename T>
-__device__ __forceinline__ void run_particle_in_place(
-    double time, double dt, int n_steps,
-    const typename T::shared_state& shared,
-    typename T::internal_state& internal, const zero_every_spec& z,
-    const std::uint64_t* zero_steps, random::rng_state& rng, double* x) {
-  for (int i = 0; i < n_steps; ++i) {
-    const double t = time + static_cast<double>(i) * dt;
-    apply_zero_every_row<T>(z, zero_steps, i, t, x);
-    T::update(t, dt, x, shared, internal, rng, x);
   }
 }
 
@@ -380,20 +292,12 @@ DUST2_PARTICLE_KERNEL(T) k_run(system_view<T> v, double time, double dt,
   const zero_every_spec& zero = mixed ? v.zero_every[g] : sm.zero;
   auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
   typename T::internal_state internal{};
-  if constexpr (smem_state<T>::enabled) {
-    double* x = state_row<T>();
-    load_state<T>(v, k, x);
-    run_particle_in_place<T>(time, dt, n_steps, shared, internal, zero,
-                             mixed ? nullptr : sm.zero_steps, rng, x);
-    store_state<T>(v, k, x);
-  } else {
-    double x[T::n_state_max];
-    double y[T::n_state_max];
-    load_state<T>(v, k, x);
-    run_particle<T>(time, dt, n_steps, shared, internal, zero,
-                    mixed ? nullptr : sm.zero_steps, rng, x, y);
-    store_state<T>(v, k, x);
-  }
+  double x[T::n_state_max];
+  double y[update_in_place_of<T>::value ? 1 : T::n_state_max];
+  load_state<T>(v, k, x);
+  run_particle<T>(time, dt, n_steps, shared, internal, zero,
+                  mixed ? nullptr : sm.zero_steps, rng, x, y);
+  store_state<T>(v, k, x);
   store_rng(v.rng, v.stride, k, rng);
   capture_error(v.errors, v.any_error, k, rng);
 }
@@ -467,9 +371,6 @@ public:
     }
     if (n_state_ > T::n_state_max) {
       throw std::runtime_error("state larger than the system's n_state_max");
-    }
-    if constexpr (has_update<T>::value && !dust2gpu::is_continuous<T>()) {
-      smem_state<T>::allow(k_run<T>, default_tile_size<T>());
     }
     DUST2_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     const int stride = layout_.stride;
@@ -661,8 +562,7 @@ public:
   void launch_run(double t0, int n_steps) {
     if constexpr (has_update<T>::value && !dust2gpu::is_continuous<T>()) {
       if (n_steps > 0) {
-        k_run<T><<<n_run_tiles(), layout_.tile_size,
-                   smem_state<T>::bytes(layout_.tile_size), stream_>>>(
+        k_run<T><<<n_run_tiles(), layout_.tile_size, 0, stream_>>>(
           run_view(), t0, dt_, n_steps);
         DUST2_CUDA(cudaGetLastError());
       }

@@ -146,24 +146,13 @@ __device__ __forceinline__ void step_compare_tile(
     const int k = tl.start + threadIdx.x;
     auto rng = load_rng(v.rng, v.stride, k, v.deterministic);
     typename T::internal_state internal{};
-    if constexpr (smem_state<T>::enabled) {
-      double* x = state_row<T>();
-      load_state<T>(v, k, x);
-      run_particle_in_place<T>(time, dt, n_steps, sm.shared(), internal,
-                               sm.zero, sm.zero_steps, rng, x);
-      logw = T::compare_data(time_compare, x, *d, sm.shared(), internal,
-                             rng);
-      store_state<T>(v, k, x);
-    } else {
-      double x[T::n_state_max];
-      double y[T::n_state_max];
-      load_state<T>(v, k, x);
-      run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
-                      sm.zero_steps, rng, x, y);
-      logw = T::compare_data(time_compare, x, *d, sm.shared(), internal,
-                             rng);
-      store_state<T>(v, k, x);
-    }
+    double x[T::n_state_max];
+    double y[update_in_place_of<T>::value ? 1 : T::n_state_max];
+    load_state<T>(v, k, x);
+    run_particle<T>(time, dt, n_steps, sm.shared(), internal, sm.zero,
+                    sm.zero_steps, rng, x, y);
+    logw = T::compare_data(time_compare, x, *d, sm.shared(), internal, rng);
+    store_state<T>(v, k, x);
     store_rng(v.rng, v.stride, k, rng);
     capture_error(v.errors, v.any_error, k, rng);
     f.w[k] = logw;
@@ -402,9 +391,6 @@ public:
                                data.size() * sizeof(data_type),
                                cudaMemcpyHostToDevice, s));
     put_rng_state(rng_words.data());
-    if constexpr (!is_continuous<T>()) {
-      smem_state<T>::allow(k_step_compare<T>, default_tile_size<T>());
-    }
     sys_->sync();
     set_fused_tail(true);
     // k_group: one warp per window of 32 chunks of the largest group
@@ -918,8 +904,7 @@ private:
         system_view<T> vs = v;
         vs.tiles = S.step_tiles_dev();
         const int step_block = S.step_block();
-        k_step_compare<T><<<S.n_step_tiles(), step_block,
-                            smem_state<T>::bytes(step_block), s>>>(
+        k_step_compare<T><<<S.n_step_tiles(), step_block, 0, s>>>(
           vs, f, st.t0, S.dt(), st.n_steps, st.t_compare,
           data_.data() + i * n_groups_data_, n_groups_data_);
       }

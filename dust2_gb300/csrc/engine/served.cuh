@@ -318,7 +318,6 @@ public:
     }
     max_tiles_ = cap_particles_ / ALIGN + n_slots_;
 
-    smem_state<T>::allow(k_served_step_compare<T>, default_tile_size<T>());
     DUST2_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     const std::size_t P = cap_particles_;
     const std::size_t S = n_slots_;
@@ -986,7 +985,7 @@ private:
     if (timed) {
       DUST2_CUDA(cudaEventRecord(r.step0, s));
     }
-    k_served_step_compare<T><<<NT, TS, smem_state<T>::bytes(TS), s>>>(
+    k_served_step_compare<T><<<NT, TS, 0, s>>>(
       sview(cur()), f, slots_dev_.data(), obs_dev_.data(), sched_.data(),
       data_.data(), slot_error_.data());
     if (timed) {

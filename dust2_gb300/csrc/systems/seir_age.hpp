@@ -23,10 +23,14 @@ struct seir_age {
   // it has written: it is correct in place, so a particle keeps one
   // state array.
   static constexpr bool update_in_place = true;
-  // the step kernels keep each particle's 96 doubles in a row of shared
-  // memory; two blocks of 128 such rows (99 KB each) fill an SM
-  static constexpr bool state_in_shared_memory = true;
-  static constexpr int min_blocks_per_sm = 2;
+  // The 96 doubles stay in a per-thread array (local memory, cached),
+  // with 4 blocks of 128 threads per SM (128 registers).  Measured on
+  // the batched SEIR filter (particle-steps/s): this 118.2M; 3 blocks
+  // 118.0M; two arrays with copies (before in-place updates), 3 blocks
+  // 116.0M; the state in rows of shared memory instead (2 blocks of 99
+  // KB per SM) 107.7M -- occupancy hides the FP64 pipe's latency better
+  // than shared memory saves local-memory traffic.
+  static constexpr int min_blocks_per_sm = 4;
   using real_type = double;
   using rng_state_type = random::rng_state;
   static constexpr int n_age = 16;
