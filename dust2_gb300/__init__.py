@@ -10,7 +10,9 @@ from .interface import (
     dust_likelihood_last_state, dust_likelihood_rng_state,
     dust_likelihood_last_snapshots, dust_likelihood_last_trajectories,
     dust_likelihood_run,
-    dust_likelihood_serial_fallbacks, dust_likelihood_server, dust_likelihood_set_rng_state, dust_ode_control,
+    dust_likelihood_serial_fallbacks, dust_likelihood_server,
+    dust_likelihood_set_rng_state, dust_likelihood_set_step_shape,
+    dust_likelihood_step_shape, dust_ode_control,
     dust_system_compare_data, dust_system_create, dust_system_internals,
     dust_system_reorder, dust_system_rng_state, dust_system_run_to_time,
     dust_system_set_rng_state, dust_system_set_state,
@@ -30,6 +32,7 @@ __all__ = [
     "dust_likelihood_last_trajectories",
     "dust_likelihood_rng_state",
     "dust_likelihood_run", "dust_likelihood_serial_fallbacks",
+    "dust_likelihood_set_step_shape", "dust_likelihood_step_shape",
     "dust_likelihood_server", "dust_likelihood_set_rng_state",
     "dust_ode_control",
     "dust_system_compare_data", "dust_system_create",

@@ -1011,6 +1011,28 @@ int dust2_gb300_filter_reorder_times(dust2_gb300_filter* filter,
   });
 }
 
+int dust2_gb300_filter_set_autotune(dust2_gb300_filter* filter,
+                                    int32_t enable) {
+  return guard([&] { filref(filter).set_autotune(enable != 0); });
+}
+
+int dust2_gb300_filter_set_step_shape(dust2_gb300_filter* filter,
+                                      int32_t block, int32_t per_tile) {
+  return guard([&] { filref(filter).set_step_shape(block, per_tile); });
+}
+
+int dust2_gb300_filter_step_shape(dust2_gb300_filter* filter, int32_t* block,
+                                  int32_t* per_tile, int32_t* n_candidates,
+                                  double* best_ms) {
+  return guard([&] {
+    int b = 0, p = 0, n = 0;
+    filref(filter).step_shape_info(&b, &p, &n, best_ms);
+    *block = b;
+    *per_tile = p;
+    *n_candidates = n;
+  });
+}
+
 int dust2_gb300_unfilter_alloc(const char* name, const double* pars,
                                size_t n_groups, size_t n_particles,
                                double time_start, const double* time,

@@ -147,6 +147,12 @@ public:
   // Device time of the reorder (state gather) launches timed the same
   // way, when the tail runs as separate kernels (else none are timed).
   virtual void reorder_times(double* ms, long* n_launches) = 0;
+  // The step kernel's launch shape (filter.cuh step_shape): tuned by
+  // timing candidates before the first run (enable), forced, or read.
+  virtual void set_autotune(bool enable) = 0;
+  virtual void set_step_shape(int block, int per_tile) = 0;
+  virtual void step_shape_info(int* block, int* per_tile, int* n_candidates,
+                               double* best_ms) = 0;
   // Save trajectories in the following runs (index_state: state entries,
   // nullptr = all); export those of the last run for `groups`, all
   // particles or select[i] of each, as [time][group][particle][state].

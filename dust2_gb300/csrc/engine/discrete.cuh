@@ -411,20 +411,6 @@ public:
     DUST2_CUDA(cudaMemcpyAsync(tiles_.data(), layout_.tiles.data(),
                                layout_.tiles.size() * sizeof(tile),
                                cudaMemcpyHostToDevice, stream_));
-    if constexpr (!dust2gpu::is_continuous<T>()) {
-      int dev = 0, sms = 0;
-      DUST2_CUDA(cudaGetDevice(&dev));
-      DUST2_CUDA(cudaDeviceGetAttribute(
-        &sms, cudaDevAttrMultiProcessorCount, dev));
-      layout_.spread_steps(4 * sms);
-      if (!layout_.step_tiles.empty()) {
-        step_tiles_.resize(layout_.step_tiles.size());
-        DUST2_CUDA(cudaMemcpyAsync(step_tiles_.data(),
-                                   layout_.step_tiles.data(),
-                                   layout_.step_tiles.size() * sizeof(tile),
-                                   cudaMemcpyHostToDevice, stream_));
-      }
-    }
     DUST2_CUDA(cudaMemcpyAsync(offsets_dev_.data(), layout_.offset.data(),
                                layout_.offset.size() * sizeof(int),
                                cudaMemcpyHostToDevice, stream_));
@@ -525,19 +511,6 @@ public:
 
   const tile* tiles_dev() const {
     return tiles_.data();
-  }
-
-  // The filter's step kernel tiles: spread one-warp tiles for small
-  // problems (group_layout::spread_steps), else the group tiles.
-  const tile* step_tiles_dev() const {
-    return layout_.step_tiles.empty() ? tiles_.data() : step_tiles_.data();
-  }
-  int n_step_tiles() const {
-    return layout_.step_tiles.empty() ? layout_.n_tiles() :
-      static_cast<int>(layout_.step_tiles.size());
-  }
-  int step_block() const {
-    return layout_.step_tiles.empty() ? layout_.tile_size : 32;
   }
   void swap_state() {
     std::swap(state_, state_other_);
@@ -806,7 +779,6 @@ private:
   device_array<shared_state> shared_dev_;
   device_array<zero_every_spec> zero_dev_;
   device_array<tile> tiles_;
-  device_array<tile> step_tiles_;
   device_array<tile> packed_;
   device_array<int> particle_group_;
   device_array<int> offsets_dev_;

@@ -104,6 +104,16 @@ struct filter_view {
 
 __global__ void k_filter_reset(filter_view f, int n_groups);
 
+// Launch shape of the filter's step kernel: group tiles of `block`
+// particles (per_tile == 0), or one-warp tiles of per_tile particles
+// (block 32).  Every shape gives the same results: the step kernel is
+// per particle, and its group reductions (any non-zero weight, maximum
+// log weight) are atomics that do not depend on order.
+struct step_shape {
+  int block;
+  int per_tile;
+};
+
 template <typename T>
 DUST2_PARTICLE_KERNEL(T) k_initial_flagged(system_view<T> v, const int* flag,
                                   double time) {
@@ -393,6 +403,9 @@ public:
     put_rng_state(rng_words.data());
     sys_->sync();
     set_fused_tail(true);
+    if constexpr (!is_continuous<T>()) {
+      set_shape(default_shape());
+    }
     // k_group: one warp per window of 32 chunks of the largest group
     int n_win = 1;
     for (int c : L.chunk_count) {
@@ -704,6 +717,11 @@ public:
     if (pending_) {
       finish(nullptr);
     }
+    if constexpr (!is_continuous<T>()) {
+      if (autotune_ && !tuned_) {
+        autotune();
+      }
+    }
     traj_current_ = false;
     snap_current_ = false;
     active_host_.assign(G, index_group == nullptr ? 1 : 0);
@@ -847,6 +865,230 @@ public:
     return random_particle_;
   }
 
+  // The step kernel's launch shape before any tuning: one-warp tiles
+  // that spread a small problem over the SM partitions (four per SM)
+  // when its group tiles would fill fewer warps than there are
+  // partitions, else the group tiles.
+  step_shape default_shape() const {
+    const auto& L = sys_->layout();
+    const int parts = 4 * n_sms();
+    long warps = 0;
+    for (int n : L.n_particles) {
+      warps += (n + 31) / 32;
+    }
+    if (warps < parts) {
+      const int per = static_cast<int>((static_cast<long>(L.n_total) +
+                                        parts - 1) / parts);
+      if (per < 32) {
+        return step_shape{32, std::max(1, per)};
+      }
+    }
+    return step_shape{L.tile_size, 0};
+  }
+
+  static int n_sms() {
+    int dev = 0, sms = 0;
+    DUST2_CUDA(cudaGetDevice(&dev));
+    DUST2_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount,
+                                      dev));
+    return sms;
+  }
+
+  void set_shape(step_shape sh) {
+    const auto& L = sys_->layout();
+    if (sh.per_tile < 0 || sh.per_tile > 32 || sh.block < 32 ||
+        sh.block % 32 != 0 || sh.block > default_tile_size<T>() ||
+        (sh.per_tile > 0 && sh.block != 32)) {
+      throw std::runtime_error("invalid step kernel shape");
+    }
+    const std::vector<tile> t = sh.per_tile > 0 ?
+      warp_tiles(L, sh.per_tile) : group_layout(L.n_particles, sh.block).tiles;
+    step_tiles_.resize(t.size());
+    DUST2_CUDA(cudaMemcpyAsync(step_tiles_.data(), t.data(),
+                               t.size() * sizeof(tile),
+                               cudaMemcpyHostToDevice, sys_->stream()));
+    n_step_tiles_ = static_cast<int>(t.size());
+    shape_ = sh;
+    graph_state_ptr_ = nullptr;  // force a re-capture
+    DUST2_CUDA(cudaStreamSynchronize(sys_->stream()));
+  }
+
+  // Candidate shapes: group tiles of every block size up to the
+  // system's, and for problems that fill fewer warps than the device has
+  // SM partitions also one-warp tiles of 1 to 16 particles.
+  std::vector<step_shape> candidates() const {
+    const auto& L = sys_->layout();
+    std::vector<step_shape> c;
+    for (int b = 32; b <= default_tile_size<T>(); b *= 2) {
+      c.push_back(step_shape{b, 0});
+    }
+    const long parts = 4L * n_sms();
+    long warps = 0;
+    for (int n : L.n_particles) {
+      warps += (n + 31) / 32;
+    }
+    if (warps < parts) {
+      for (int per = 1; per <= 16; per *= 2) {
+        if (static_cast<long>(warp_tiles(L, per).size()) <= 4 * parts) {
+          c.push_back(step_shape{32, per});
+        }
+      }
+    }
+    return c;
+  }
+
+  // Pick the fastest candidate shape by timing the step kernel on
+  // scratch copies of the particles: initial conditions, advanced part
+  // of the way into the schedule (the cost of a step depends on the
+  // state), then one observation's steps per candidate, three times,
+  // keeping each candidate's fastest.  The filter's own state,
+  // generators and error records are not touched; its weights and group
+  // reductions are reset by the run that follows.  Skipped when the
+  // scratch copies would take more than a quarter of the free memory.
+  void autotune() {
+    tuned_ = true;
+    auto& S = *sys_;
+    const auto& L = S.layout();
+    const auto cand = candidates();
+    n_candidates_ = static_cast<int>(cand.size());
+    if (cand.size() < 2 || schedule_.empty()) {
+      return;
+    }
+    const std::size_t n_st = static_cast<std::size_t>(S.n_state()) *
+      L.stride;
+    const std::size_t bytes = 2 * n_st * sizeof(double) +
+      8 * static_cast<std::size_t>(L.stride) * sizeof(std::uint64_t) +
+      L.n_total * sizeof(particle_error);
+    std::size_t free_b = 0, total_b = 0;
+    DUST2_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    if (bytes > free_b / 4) {
+      return;
+    }
+    auto s = S.stream();
+    device_array<double> base(n_st), work(n_st);
+    device_array<std::uint64_t> rng_base(4 * L.stride), rng_work(4 * L.stride);
+    device_array<particle_error> err(L.n_total);
+    device_array<int> any(1);
+    system_view<T> v = S.run_view();
+    DUST2_CUDA(cudaMemcpyAsync(base.data(), v.state, n_st * sizeof(double),
+                               cudaMemcpyDeviceToDevice, s));
+    DUST2_CUDA(cudaMemcpyAsync(rng_base.data(), v.rng,
+                               4 * L.stride * sizeof(std::uint64_t),
+                               cudaMemcpyDeviceToDevice, s));
+    v.state = base.data();
+    v.rng = rng_base.data();
+    v.errors = err.data();
+    v.any_error = any.data();
+    const int run_tiles = S.n_run_tiles();
+    k_initial<T><<<run_tiles, L.tile_size, 0, s>>>(v, nullptr, time_start_);
+    // part of the way in: half the schedule's steps, at most 100
+    const std::size_t mid = schedule_.size() / 2;
+    int steps = 0;
+    for (std::size_t i = 0; i < mid; ++i) {
+      steps += schedule_[i].n_steps;
+    }
+    steps = std::min(steps, 100);
+    if (steps > 0) {
+      k_run<T><<<run_tiles, L.tile_size, 0, s>>>(v, time_start_, S.dt(),
+                                                 steps);
+    }
+    DUST2_CUDA(cudaGetLastError());
+    const double t0 = time_start_ + steps * S.dt();
+    const int n_steps = std::max(1, schedule_[mid].n_steps);
+    const auto* d = data_.data() + mid * n_groups_data_;
+    filter_view f = view();
+    active_host_.assign(L.n_groups, 1);
+    DUST2_CUDA(cudaMemcpyAsync(active_.data(), active_host_.data(),
+                               L.n_groups * sizeof(int),
+                               cudaMemcpyHostToDevice, s));
+    std::vector<device_array<tile>> tiles(cand.size());
+    std::vector<int> n_tiles(cand.size());
+    for (std::size_t c = 0; c < cand.size(); ++c) {
+      const std::vector<tile> t = cand[c].per_tile > 0 ?
+        warp_tiles(L, cand[c].per_tile) :
+        group_layout(L.n_particles, cand[c].block).tiles;
+      tiles[c].resize(t.size());
+      DUST2_CUDA(cudaMemcpyAsync(tiles[c].data(), t.data(),
+                                 t.size() * sizeof(tile),
+                                 cudaMemcpyHostToDevice, s));
+      n_tiles[c] = static_cast<int>(t.size());
+    }
+    constexpr int REPS = 3;
+    std::vector<cudaEvent_t> ev(2 * REPS * cand.size());
+    for (auto& e : ev) {
+      DUST2_CUDA(cudaEventCreate(&e));
+    }
+    system_view<T> w = S.view();
+    w.state = work.data();
+    w.rng = rng_work.data();
+    w.errors = err.data();
+    w.any_error = any.data();
+    for (int r = 0; r < REPS; ++r) {
+      for (std::size_t c = 0; c < cand.size(); ++c) {
+        DUST2_CUDA(cudaMemcpyAsync(work.data(), base.data(),
+                                   n_st * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+        DUST2_CUDA(cudaMemcpyAsync(rng_work.data(), rng_base.data(),
+                                   4 * L.stride * sizeof(std::uint64_t),
+                                   cudaMemcpyDeviceToDevice, s));
+        w.tiles = tiles[c].data();
+        const std::size_t e = 2 * (r * cand.size() + c);
+        DUST2_CUDA(cudaEventRecord(ev[e], s));
+        k_step_compare<T><<<n_tiles[c], cand[c].block, 0, s>>>(
+          w, f, t0, S.dt(), n_steps, t0 + n_steps * S.dt(), d,
+          n_groups_data_);
+        DUST2_CUDA(cudaEventRecord(ev[e + 1], s));
+      }
+    }
+    DUST2_CUDA(cudaGetLastError());
+    DUST2_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> best(cand.size(), 1e300);
+    for (int r = 0; r < REPS; ++r) {
+      for (std::size_t c = 0; c < cand.size(); ++c) {
+        const std::size_t e = 2 * (r * cand.size() + c);
+        float ms = 0;
+        DUST2_CUDA(cudaEventElapsedTime(&ms, ev[e], ev[e + 1]));
+        best[c] = std::min(best[c], static_cast<double>(ms));
+      }
+    }
+    for (auto e : ev) {
+      cudaEventDestroy(e);
+    }
+    const std::size_t pick = static_cast<std::size_t>(
+      std::min_element(best.begin(), best.end()) - best.begin());
+    best_ms_ = best[pick];
+    set_shape(cand[pick]);
+  }
+
+  void set_autotune(bool enable) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    autotune_ = enable;
+  }
+
+  void set_step_shape(int block, int per_tile) override {
+    if (pending_) {
+      finish(nullptr);
+    }
+    if constexpr (is_continuous<T>()) {
+      throw std::runtime_error("the step shape applies to discrete-time "
+                               "filters");
+    } else {
+      set_shape(step_shape{block, per_tile});
+      autotune_ = false;
+      tuned_ = true;
+    }
+  }
+
+  void step_shape_info(int* block, int* per_tile, int* n_candidates,
+                       double* best_ms) override {
+    *block = shape_.block;
+    *per_tile = shape_.per_tile;
+    *n_candidates = n_candidates_;
+    *best_ms = best_ms_;
+  }
+
   ~filter_engine() override {
     cudaStreamSynchronize(sys_->stream());
     for (auto e : ev_step_) {
@@ -902,9 +1144,8 @@ private:
           data_.data() + i * n_groups_data_, n_groups_data_);
       } else {
         system_view<T> vs = v;
-        vs.tiles = S.step_tiles_dev();
-        const int step_block = S.step_block();
-        k_step_compare<T><<<S.n_step_tiles(), step_block, 0, s>>>(
+        vs.tiles = step_tiles_.data();
+        k_step_compare<T><<<n_step_tiles_, shape_.block, 0, s>>>(
           vs, f, st.t0, S.dt(), st.n_steps, st.t_compare,
           data_.data() + i * n_groups_data_, n_groups_data_);
       }
@@ -1098,6 +1339,15 @@ private:
   device_array<int> fallback_count_;
   device_array<int> force_serial_;
   device_array<data_type> data_;
+
+  // launch shape of the step kernel (discrete-time systems)
+  step_shape shape_{};
+  device_array<tile> step_tiles_;
+  int n_step_tiles_ = 0;
+  bool autotune_ = true;
+  bool tuned_ = false;
+  int n_candidates_ = 0;
+  double best_ms_ = 0;
 
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;

@@ -115,46 +115,27 @@ struct group_layout {
     return use_packed ? packed : tiles;
   }
 
-  // Spread tiles for the filter's step kernel when the particles fill
-  // fewer warps than the device has SM partitions (n_partitions: four
-  // per SM).  Each partition issues one FP64 warp instruction every 64
-  // cycles however many lanes are active, so a warp's time is its FP64
-  // instruction count, and that grows with the divergence of its lanes.
-  // A small filter then runs faster with fewer particles per warp, one
-  // warp per partition: step_tiles are one-warp tiles of at most
-  // step_per_tile particles (never spanning two groups).  Empty when the
-  // problem is large enough to fill the device with full warps.
-  std::vector<tile> step_tiles;
-  int step_per_tile = 0;
-
-  void spread_steps(int n_partitions) {
-    step_tiles.clear();
-    step_per_tile = 0;
-    long warps = 0;
-    for (int n : n_particles) {
-      warps += (n + 31) / 32;
-    }
-    if (n_partitions <= 0 || warps >= n_partitions) {
-      return;
-    }
-    const int per = static_cast<int>(
-      (static_cast<long>(n_total) + n_partitions - 1) / n_partitions);
-    if (per >= 32) {
-      return;
-    }
-    step_per_tile = std::max(1, per);
-    for (int g = 0; g < n_groups; ++g) {
-      for (int local = 0; local < n_particles[g]; local += step_per_tile) {
-        const int count = std::min(step_per_tile, n_particles[g] - local);
-        step_tiles.push_back(tile{g, offset[g] + local, count, local});
-      }
-    }
-  }
-
   int n_tiles() const {
     return static_cast<int>(tiles.size());
   }
 };
+
+// One-warp tiles of at most `per_tile` particles each (never spanning two
+// groups), for the filter's step kernel on small problems: a warp issues
+// one FP64 instruction per 64 cycles of its SM partition however many of
+// its lanes are active, so a warp's time is its FP64 instruction count,
+// which grows with the divergence of its lanes; with fewer particles per
+// warp, one warp per partition, a small filter steps faster.
+inline std::vector<tile> warp_tiles(const group_layout& L, int per_tile) {
+  std::vector<tile> out;
+  for (int g = 0; g < L.n_groups; ++g) {
+    for (int local = 0; local < L.n_particles[g]; local += per_tile) {
+      const int count = std::min(per_tile, L.n_particles[g] - local);
+      out.push_back(tile{g, L.offset[g] + local, count, local});
+    }
+  }
+  return out;
+}
 
 }  // namespace engine
 }  // namespace dust2gpu

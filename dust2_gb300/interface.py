@@ -761,6 +761,7 @@ class DustLikelihood:
         # run options, applied to the engine object when it is created
         self.serial_resample = False
         self.fused_tail = True
+        self.step_shape = None  # (block, per_tile) forced, else tuned
 
     @property
     def ptr(self):
@@ -772,6 +773,11 @@ class DustLikelihood:
             self._handle, 1 if self.serial_resample else 0))
         check(lib.dust2_gb300_filter_set_fused_tail(
             self._handle, 1 if self.fused_tail else 0))
+        if self.step_shape is not None and \
+                self.generator.time_type == "discrete":
+            check(lib.dust2_gb300_filter_set_step_shape(
+                self._handle, int(self.step_shape[0]),
+                int(self.step_shape[1])))
 
     def initialise(self, pars):
         flat = as_f64(np.concatenate([self.generator.pack_pars(p)
@@ -1283,6 +1289,32 @@ def dust_likelihood_last_state(obj, select_random_particle=False):
     if obj.preserve_group_dimension:
         return arr
     return arr[:, :, 0]
+
+
+def dust_likelihood_set_step_shape(obj, block, per_tile=0):
+    """Force the step kernel's launch shape of a discrete-time filter:
+    group tiles of `block` threads (per_tile 0) or one-warp tiles of
+    per_tile particles (block 32); turns the autotuner off.  Results do
+    not depend on it."""
+    _check_lik(obj)
+    obj.step_shape = (int(block), int(per_tile))
+    if obj.ptr is not None:
+        obj.apply_options()
+
+
+def dust_likelihood_step_shape(obj):
+    """The step kernel's launch shape in use: block, per_tile, the number
+    of candidates the autotuner timed and the chosen one's time (ms)."""
+    _check_lik(obj)
+    if obj.ptr is None:
+        raise DustError("The filter has not run yet")
+    b, p, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    ms = ctypes.c_double()
+    check(_lib.lib().dust2_gb300_filter_step_shape(
+        obj.ptr, ctypes.byref(b), ctypes.byref(p), ctypes.byref(n),
+        ctypes.byref(ms)))
+    return {"block": b.value, "per_tile": p.value, "n_candidates": n.value,
+            "best_ms": ms.value}
 
 
 def resample_weight(w, u):

@@ -430,3 +430,47 @@ def test_scale_log_weights_hook(port):
     rp, wp = port.scale_log_weights(x)
     assert abs(r - rp) <= 1e-12 * abs(rp)
     np.testing.assert_allclose(w, wp, rtol=4.5e-16, atol=1e-300)
+
+
+def test_step_shapes_give_identical_results(port):
+    """Every launch shape of the step kernel (group tiles of 32-256
+    threads, one-warp tiles of 1-16 particles) gives the same
+    log-likelihoods, state and generators, equal to the oracle's; the
+    autotuner times the candidates and keeps one of them."""
+    gen = d.sir_cases()
+    npg = [700, 33, 1500]
+    rs = np.random.default_rng(8)
+    plist = [{"beta": 0.2 + 0.1 * g, "gamma": 0.1, "N": 1e4, "I0": 10}
+             for g in range(3)]
+    times = np.arange(1, 31, dtype=float)
+    data = rs.poisson(20, (times.size, 3)).astype(float)
+    cols = {"time": np.repeat(times, 3), "incidence": data.ravel(),
+            "group": np.tile(np.arange(1, 4), times.size)}
+    results = []
+    for shape in [(32, 0), (64, 0), (128, 0), (256, 0), (32, 1), (32, 3),
+                  (32, 16), None]:
+        obj = d.dust_filter_create(gen, 0, cols, n_particles=npg, dt=0.25,
+                                   seed=21)
+        if shape is not None:
+            d.dust_likelihood_set_step_shape(obj, *shape)
+        words = np.frombuffer(d.dust_likelihood_rng_state(obj), dtype="<u8")
+        ll = d.dust_likelihood_run(obj, plist)
+        state = np.asarray(d.dust_likelihood_last_state(obj)).ravel()
+        rng = np.frombuffer(d.dust_likelihood_rng_state(obj), dtype="<u8")
+        info = d.dust_likelihood_step_shape(obj)
+        if shape is not None:
+            assert (info["block"], info["per_tile"]) == shape
+            assert info["n_candidates"] == 0
+        else:
+            assert info["n_candidates"] >= 4  # tuned among the candidates
+            assert info["best_ms"] > 0
+        results.append((ll, state, rng))
+    flat = np.concatenate([gen.pack_pars(p) for p in plist])
+    want, want_state, want_rng = port.filter_run(
+        "sir_cases", flat, npg, 0.0, times, data.ravel(), 3, 0.25, words,
+        n_state=4)
+    for ll, state, rng in results:
+        np.testing.assert_allclose(ll, want[0], rtol=1e-12, atol=0)
+        np.testing.assert_array_equal(ll, results[0][0])
+        np.testing.assert_array_equal(state, want_state[:sum(npg) * 4])
+        np.testing.assert_array_equal(rng, want_rng)
