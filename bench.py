@@ -71,6 +71,28 @@ FP64_PIPE_INST_PER_UNIT = {"sir_batched": 162.7, "seir_batched": 2682.7,
                            "ode_batched": 641.3}
 
 
+# A second basis for the FP64 roofline, independent of moving work off
+# the FP64 pipe: the FP64 operations (DADD + DMUL + 2 DFMA) the same step
+# kernel executed per particle-step when exp and log were still evaluated
+# in FP64 (Tang's table methods), measured by ncu on that build (whole
+# runs of the batched workloads).  The integer fixed-point exp and log of
+# the current build compute the same values with no FP64 instruction, so
+# this counts the FP64 work of the algorithm as a plain FP64
+# implementation would issue it.
+FP64_FORMULATION_OPS = {"sir_batched": 259.6, "seir_batched": 4552.2}
+
+
+def formulation_roofline(workload, units_per_s, peak_tflops):
+    ops = FP64_FORMULATION_OPS.get(workload)
+    if ops is None or not units_per_s:
+        return None
+    achieved = ops * units_per_s / 1e12
+    return {"flops_per_unit": ops, "achieved": achieved,
+            "frac": achieved / peak_tflops, "unit": "TFLOP/s",
+            "basis": "FP64 ops per particle-step of the step kernel with "
+                     "exp/log in FP64 (ncu, earlier build)"}
+
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
 # same kernel, from the same captures; `traffic` is this times the units
 # of one launch.
@@ -500,6 +522,8 @@ def gpu_arm(args, rank, world, local):
             "step_launch_ms": step_launch_ms,
             "fp64_pipe": pipe_roofline(
                 args.workload, ps_per_launch / (step_launch_ms * 1e-3), peak),
+            "fp64_formulation": formulation_roofline(
+                args.workload, ps_per_launch / (step_launch_ms * 1e-3), peak),
             "step_share_of_run": step_ms.value / max(run_ms.value, 1e-12),
             "flops_basis": "executed FP64 ops per particle-step (ncu SASS "
                            "dadd+dmul+2*dfma)"}
@@ -824,6 +848,8 @@ def serve_arm(args, rank, world, local):
                            "has no FP64 entry",
             "step_kernel_share": step_ms * 1e-3 / served_s,
             "fp64_pipe": pipe_roofline("seir_batched", in_kernel_rate, peak),
+            "fp64_formulation": formulation_roofline("seir_batched",
+                                                     in_kernel_rate, peak),
             "flops_basis": "executed FP64 ops per particle-step of the "
                            "SEIR step kernel (ncu SASS dadd+dmul+2*dfma)"},
     }
