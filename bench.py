@@ -94,9 +94,11 @@ def formulation_roofline(workload, units_per_s, peak_tflops):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
-# same kernel, from the same captures; `traffic` is this times the units
+# same kernel, from ncu captures (SIR and dopri5: whole runs; SEIR: one
+# launch at observation 200 of the current build, which keeps the state
+# in a per-thread local-memory array); `traffic` is this times the units
 # of one launch.
-DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2653.4,
+DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2447.0,
                        "ode_batched": 40.0}
 
 
@@ -515,7 +517,7 @@ def gpu_arm(args, rank, world, local):
             "traffic": traffic_per_launch(args.workload, ps_per_launch),
             "traffic_source": "ncu dram__bytes_read.sum + "
                               "dram__bytes_write.sum per particle-step of "
-                              "this kernel over a whole run, times the "
+                              "this kernel (DRAM_BYTES_PER_UNIT), times the "
                               "particle-steps of one launch",
             "peak_source": "measured in-process: DFMA-chain microbenchmark "
                            "(dust2_gb300_fp64_peak); MEASURED_PEAKS.json has no FP64 entry",
@@ -548,6 +550,8 @@ def gpu_arm(args, rank, world, local):
             "clocks": clock_info,
             "roofline": roofline,
             "serial_fallbacks": d.dust_likelihood_serial_fallbacks(obj),
+            # the step kernel's launch shape chosen by the autotuner
+            "step_shape": d.dust_likelihood_step_shape(obj),
             "reorder_roofline": reorder_roofline(
                 n_total, w["n_state"], reorder_ms.value, n_reorder.value),
         }
@@ -1036,10 +1040,13 @@ def reference_arm(args, rank, world):
     port = pyoracle.port_timing()
     threads = port.max_threads()
     unit = "particle-steps/s"
+    # each of the warmup + steps runs is one sample of about a third of
+    # the CPU-baseline target, so that 25 runs take a couple of minutes
+    step_seconds = args.cpu_seconds / 3
     if args.workload == "ode_batched":
         from dust2_gb300 import workloads
         w = workloads.sirode_batched(n_instances=args.ode_instances)
-        base = ode_cpu_baseline(w, args.cpu_seconds)
+        base = ode_cpu_baseline(w, step_seconds)
         n_inst = base["instances"]
 
         def one():
@@ -1049,7 +1056,7 @@ def reference_arm(args, rank, world):
     elif args.workload == "serve_seir":
         w = serve_workload(oracle_simulate(), args.steps,
                            packer=pyoracle.pack_pars)
-        picks, base = serve_cpu_sample(w, args.cpu_seconds, threads)
+        picks, base = serve_cpu_sample(w, step_seconds, threads)
 
         def one():
             return serve_cpu_run(w, picks, threads)
@@ -1058,7 +1065,7 @@ def reference_arm(args, rank, world):
     else:
         w = build_workload(args.workload, oracle_simulate(),
                            packer=pyoracle.pack_pars)
-        n_groups = cpu_sample_groups(w, args.cpu_seconds, threads)
+        n_groups = cpu_sample_groups(w, step_seconds, threads)
         base = {"sample": cpu_sample_text(w, n_groups)}
 
         def one():
