@@ -144,11 +144,11 @@ _SIGNATURES = {
     "dust2_gb300_filter_set_autotune": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.c_int32]),
     "dust2_gb300_filter_set_step_shape": (ctypes.c_int, [
-        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]),
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "dust2_gb300_filter_step_shape": (ctypes.c_int, [
         ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
-        c_double_p]),
+        ctypes.POINTER(ctypes.c_int32), c_double_p]),
     "dust2_gb300_system_simulate_device": (ctypes.c_int, [
         ctypes.c_void_p, c_double_p, ctypes.c_size_t, ctypes.c_void_p]),
     "dust2_gb300_system_stream": (ctypes.c_int, [ctypes.c_void_p,

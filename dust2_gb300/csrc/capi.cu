@@ -1017,18 +1017,22 @@ int dust2_gb300_filter_set_autotune(dust2_gb300_filter* filter,
 }
 
 int dust2_gb300_filter_set_step_shape(dust2_gb300_filter* filter,
-                                      int32_t block, int32_t per_tile) {
-  return guard([&] { filref(filter).set_step_shape(block, per_tile); });
+                                      int32_t block, int32_t per_tile,
+                                      int32_t persistent) {
+  return guard([&] {
+    filref(filter).set_step_shape(block, per_tile, persistent != 0);
+  });
 }
 
 int dust2_gb300_filter_step_shape(dust2_gb300_filter* filter, int32_t* block,
-                                  int32_t* per_tile, int32_t* n_candidates,
-                                  double* best_ms) {
+                                  int32_t* per_tile, int32_t* persistent,
+                                  int32_t* n_candidates, double* best_ms) {
   return guard([&] {
-    int b = 0, p = 0, n = 0;
-    filref(filter).step_shape_info(&b, &p, &n, best_ms);
+    int b = 0, p = 0, q = 0, n = 0;
+    filref(filter).step_shape_info(&b, &p, &q, &n, best_ms);
     *block = b;
     *per_tile = p;
+    *persistent = q;
     *n_candidates = n;
   });
 }

@@ -150,9 +150,9 @@ public:
   // The step kernel's launch shape (filter.cuh step_shape): tuned by
   // timing candidates before the first run (enable), forced, or read.
   virtual void set_autotune(bool enable) = 0;
-  virtual void set_step_shape(int block, int per_tile) = 0;
-  virtual void step_shape_info(int* block, int* per_tile, int* n_candidates,
-                               double* best_ms) = 0;
+  virtual void set_step_shape(int block, int per_tile, bool persistent) = 0;
+  virtual void step_shape_info(int* block, int* per_tile, int* persistent,
+                               int* n_candidates, double* best_ms) = 0;
   // Save trajectories in the following runs (index_state: state entries,
   // nullptr = all); export those of the last run for `groups`, all
   // particles or select[i] of each, as [time][group][particle][state].

@@ -106,12 +106,15 @@ __global__ void k_filter_reset(filter_view f, int n_groups);
 
 // Launch shape of the filter's step kernel: group tiles of `block`
 // particles (per_tile == 0), or one-warp tiles of per_tile particles
-// (block 32).  Every shape gives the same results: the step kernel is
-// per particle, and its group reductions (any non-zero weight, maximum
-// log weight) are atomics that do not depend on order.
+// (block 32); one block per tile, or (persistent) a grid that fills the
+// device once and takes tiles from a device work queue.  Every shape
+// gives the same results: the step kernel is per particle, and its group
+// reductions (any non-zero weight, maximum log weight) are atomics that
+// do not depend on order.
 struct step_shape {
   int block;
   int per_tile;
+  bool persistent;
 };
 
 template <typename T>
@@ -260,6 +263,39 @@ DUST2_PARTICLE_KERNEL(T) k_step_compare(system_view<T> v, filter_view f,
                        data + (n_groups_data == 1 ? 0 : tl.group));
 }
 
+// k_step_compare as a persistent kernel: a grid sized to fill the device
+// once, whose blocks take tiles in order from a device work queue (an
+// atomic counter, zero before the launch) until none are left.  Tiles of
+// groups of very different sizes then share one launch without a block
+// per tile, and a block that finishes early takes the next tile at once.
+template <typename T>
+DUST2_PARTICLE_KERNEL(T) k_step_compare_queue(
+    system_view<T> v, filter_view f, double time, double dt, int n_steps,
+    double time_compare, const typename T::data_type* data,
+    int n_groups_data, int n_tiles, int* next_tile) {
+  __shared__ shared_smem<T> sm;
+  __shared__ double red[33];
+  __shared__ int taken;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      taken = atomicAdd(next_tile, 1);
+    }
+    __syncthreads();
+    const int t = taken;
+    __syncthreads();  // every thread has read `taken` before it changes
+    if (t >= n_tiles) {
+      return;
+    }
+    const tile tl = v.tiles[t];
+    if (!f.active[tl.group]) {
+      continue;
+    }
+    step_compare_tile<T>(v, f, tl, sm, red, time, dt, n_steps,
+                         time_compare,
+                         data + (n_groups_data == 1 ? 0 : tl.group));
+  }
+}
+
 // Exclusive offsets of a group's chunks (warp scans of 32 chunk totals
 // and a running carry; the exclusive value comes from the neighbour
 // lane, so every offset is a plain sum); returns the group total.
@@ -404,6 +440,7 @@ public:
     sys_->sync();
     set_fused_tail(true);
     if constexpr (!is_continuous<T>()) {
+      queue_.resize(std::max<std::size_t>(1, schedule_.size()));
       set_shape(default_shape());
     }
     // k_group: one warp per window of 32 chunks of the largest group
@@ -880,10 +917,53 @@ public:
       const int per = static_cast<int>((static_cast<long>(L.n_total) +
                                         parts - 1) / parts);
       if (per < 32) {
-        return step_shape{32, std::max(1, per)};
+        return step_shape{32, std::max(1, per), false};
       }
     }
-    return step_shape{L.tile_size, 0};
+    return step_shape{L.tile_size, 0, false};
+  }
+
+  // Blocks of a persistent step launch: as many as fit on the device at
+  // once (at most one per tile).
+  int persistent_grid(int block, int n_tiles) const {
+    int per_sm = 0;
+    DUST2_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, k_step_compare_queue<T>, block, 0));
+    return std::max(1, std::min(n_tiles, std::max(1, per_sm) * n_sms()));
+  }
+
+  // One step+compare launch of observation i in the current shape, on
+  // the given state and generators (the filter's, or the autotuner's
+  // scratch copies); `next_tile` is the zeroed work-queue counter of a
+  // persistent launch.
+  void launch_step(cudaStream_t s, const filter_view& f, double* state,
+                   std::uint64_t* rng, const obs_step& st, std::size_t i,
+                   int* next_tile) {
+    auto& S = *sys_;
+    system_view<T> v = S.view();
+    v.state = state;
+    v.rng = rng;
+    v.tiles = step_tiles_.data();
+    launch_step_shape(s, f, v, shape_, n_step_tiles_, step_grid_, st, i,
+                      next_tile);
+  }
+
+  // `grid`: the blocks of a persistent launch (persistent_grid, found
+  // before any graph capture).
+  void launch_step_shape(cudaStream_t s, const filter_view& f,
+                         const system_view<T>& v, const step_shape& sh,
+                         int n_tiles, int grid, const obs_step& st,
+                         std::size_t i, int* next_tile) {
+    auto& S = *sys_;
+    const auto* d = data_.data() + i * n_groups_data_;
+    if (sh.persistent) {
+      k_step_compare_queue<T><<<grid, sh.block, 0, s>>>(
+        v, f, st.t0, S.dt(), st.n_steps, st.t_compare, d, n_groups_data_,
+        n_tiles, next_tile);
+    } else {
+      k_step_compare<T><<<n_tiles, sh.block, 0, s>>>(
+        v, f, st.t0, S.dt(), st.n_steps, st.t_compare, d, n_groups_data_);
+    }
   }
 
   static int n_sms() {
@@ -908,6 +988,8 @@ public:
                                t.size() * sizeof(tile),
                                cudaMemcpyHostToDevice, sys_->stream()));
     n_step_tiles_ = static_cast<int>(t.size());
+    step_grid_ = sh.persistent ? persistent_grid(sh.block, n_step_tiles_) :
+      n_step_tiles_;
     shape_ = sh;
     graph_state_ptr_ = nullptr;  // force a re-capture
     DUST2_CUDA(cudaStreamSynchronize(sys_->stream()));
@@ -920,7 +1002,8 @@ public:
     const auto& L = sys_->layout();
     std::vector<step_shape> c;
     for (int b = 32; b <= default_tile_size<T>(); b *= 2) {
-      c.push_back(step_shape{b, 0});
+      c.push_back(step_shape{b, 0, false});
+      c.push_back(step_shape{b, 0, true});
     }
     const long parts = 4L * n_sms();
     long warps = 0;
@@ -930,7 +1013,7 @@ public:
     if (warps < parts) {
       for (int per = 1; per <= 16; per *= 2) {
         if (static_cast<long>(warp_tiles(L, per).size()) <= 4 * parts) {
-          c.push_back(step_shape{32, per});
+          c.push_back(step_shape{32, per, false});
         }
       }
     }
@@ -995,7 +1078,8 @@ public:
     DUST2_CUDA(cudaGetLastError());
     const double t0 = time_start_ + steps * S.dt();
     const int n_steps = std::max(1, schedule_[mid].n_steps);
-    const auto* d = data_.data() + mid * n_groups_data_;
+    const obs_step trial{t0, n_steps, t0 + n_steps * S.dt()};
+    device_array<int> counter(1);
     filter_view f = view();
     active_host_.assign(L.n_groups, 1);
     DUST2_CUDA(cudaMemcpyAsync(active_.data(), active_host_.data(),
@@ -1003,6 +1087,7 @@ public:
                                cudaMemcpyHostToDevice, s));
     std::vector<device_array<tile>> tiles(cand.size());
     std::vector<int> n_tiles(cand.size());
+    std::vector<int> grids(cand.size());
     for (std::size_t c = 0; c < cand.size(); ++c) {
       const std::vector<tile> t = cand[c].per_tile > 0 ?
         warp_tiles(L, cand[c].per_tile) :
@@ -1012,6 +1097,8 @@ public:
                                  t.size() * sizeof(tile),
                                  cudaMemcpyHostToDevice, s));
       n_tiles[c] = static_cast<int>(t.size());
+      grids[c] = cand[c].persistent ?
+        persistent_grid(cand[c].block, n_tiles[c]) : n_tiles[c];
     }
     constexpr int REPS = 3;
     std::vector<cudaEvent_t> ev(2 * REPS * cand.size());
@@ -1031,12 +1118,12 @@ public:
         DUST2_CUDA(cudaMemcpyAsync(rng_work.data(), rng_base.data(),
                                    4 * L.stride * sizeof(std::uint64_t),
                                    cudaMemcpyDeviceToDevice, s));
+        DUST2_CUDA(cudaMemsetAsync(counter.data(), 0, sizeof(int), s));
         w.tiles = tiles[c].data();
         const std::size_t e = 2 * (r * cand.size() + c);
         DUST2_CUDA(cudaEventRecord(ev[e], s));
-        k_step_compare<T><<<n_tiles[c], cand[c].block, 0, s>>>(
-          w, f, t0, S.dt(), n_steps, t0 + n_steps * S.dt(), d,
-          n_groups_data_);
+        launch_step_shape(s, f, w, cand[c], n_tiles[c], grids[c], trial,
+                          mid, counter.data());
         DUST2_CUDA(cudaEventRecord(ev[e + 1], s));
       }
     }
@@ -1067,7 +1154,7 @@ public:
     autotune_ = enable;
   }
 
-  void set_step_shape(int block, int per_tile) override {
+  void set_step_shape(int block, int per_tile, bool persistent) override {
     if (pending_) {
       finish(nullptr);
     }
@@ -1075,16 +1162,17 @@ public:
       throw std::runtime_error("the step shape applies to discrete-time "
                                "filters");
     } else {
-      set_shape(step_shape{block, per_tile});
+      set_shape(step_shape{block, per_tile, persistent});
       autotune_ = false;
       tuned_ = true;
     }
   }
 
-  void step_shape_info(int* block, int* per_tile, int* n_candidates,
-                       double* best_ms) override {
+  void step_shape_info(int* block, int* per_tile, int* persistent,
+                       int* n_candidates, double* best_ms) override {
     *block = shape_.block;
     *per_tile = shape_.per_tile;
+    *persistent = shape_.persistent ? 1 : 0;
     *n_candidates = n_candidates_;
     *best_ms = best_ms_;
   }
@@ -1125,6 +1213,13 @@ private:
       record(ev_run_[0]);
     }
     k_filter_reset<<<n_blocks(G, 128), 128, 0, s>>>(f, G);
+    if constexpr (!is_continuous<T>()) {
+      if (shape_.persistent) {
+        // one work-queue counter per data time, all zero before the run
+        DUST2_CUDA(cudaMemsetAsync(queue_.data(), 0,
+                                   schedule_.size() * sizeof(int), s));
+      }
+    }
     DUST2_CUDA(cudaMemsetAsync(fallback_count_.data(), 0, G * sizeof(int), s));
     system_view<T> v = S.view();
     k_initial_flagged<T><<<NT, TS, 0, s>>>(v, set_initial_.data(),
@@ -1143,11 +1238,7 @@ private:
           st.t_compare, owner_->dt(), i == 0 ? 1 : 0,
           data_.data() + i * n_groups_data_, n_groups_data_);
       } else {
-        system_view<T> vs = v;
-        vs.tiles = step_tiles_.data();
-        k_step_compare<T><<<n_step_tiles_, shape_.block, 0, s>>>(
-          vs, f, st.t0, S.dt(), st.n_steps, st.t_compare,
-          data_.data() + i * n_groups_data_, n_groups_data_);
+        launch_step(s, f, v.state, v.rng, st, i, queue_.data() + i);
       }
       if (timing_) {
         record(ev_step_[2 * i + 1]);
@@ -1342,7 +1433,9 @@ private:
 
   // launch shape of the step kernel (discrete-time systems)
   step_shape shape_{};
+  int step_grid_ = 0;
   device_array<tile> step_tiles_;
+  device_array<int> queue_;  // [n_times] work-queue counters
   int n_step_tiles_ = 0;
   bool autotune_ = true;
   bool tuned_ = false;

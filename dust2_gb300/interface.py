@@ -777,7 +777,7 @@ class DustLikelihood:
                 self.generator.time_type == "discrete":
             check(lib.dust2_gb300_filter_set_step_shape(
                 self._handle, int(self.step_shape[0]),
-                int(self.step_shape[1])))
+                int(self.step_shape[1]), int(bool(self.step_shape[2]))))
 
     def initialise(self, pars):
         flat = as_f64(np.concatenate([self.generator.pack_pars(p)
@@ -1291,29 +1291,32 @@ def dust_likelihood_last_state(obj, select_random_particle=False):
     return arr[:, :, 0]
 
 
-def dust_likelihood_set_step_shape(obj, block, per_tile=0):
+def dust_likelihood_set_step_shape(obj, block, per_tile=0, persistent=False):
     """Force the step kernel's launch shape of a discrete-time filter:
     group tiles of `block` threads (per_tile 0) or one-warp tiles of
-    per_tile particles (block 32); turns the autotuner off.  Results do
-    not depend on it."""
+    per_tile particles (block 32), one block per tile or (persistent) a
+    device-filling grid taking tiles from a work queue; turns the
+    autotuner off.  Results do not depend on it."""
     _check_lik(obj)
-    obj.step_shape = (int(block), int(per_tile))
+    obj.step_shape = (int(block), int(per_tile), bool(persistent))
     if obj.ptr is not None:
         obj.apply_options()
 
 
 def dust_likelihood_step_shape(obj):
-    """The step kernel's launch shape in use: block, per_tile, the number
-    of candidates the autotuner timed and the chosen one's time (ms)."""
+    """The step kernel's launch shape in use: block, per_tile, persistent,
+    the number of candidates the autotuner timed and the chosen one's
+    time (ms)."""
     _check_lik(obj)
     if obj.ptr is None:
         raise DustError("The filter has not run yet")
-    b, p, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    b, p, q, n = (ctypes.c_int32() for _ in range(4))
     ms = ctypes.c_double()
     check(_lib.lib().dust2_gb300_filter_step_shape(
-        obj.ptr, ctypes.byref(b), ctypes.byref(p), ctypes.byref(n),
-        ctypes.byref(ms)))
-    return {"block": b.value, "per_tile": p.value, "n_candidates": n.value,
+        obj.ptr, ctypes.byref(b), ctypes.byref(p), ctypes.byref(q),
+        ctypes.byref(n), ctypes.byref(ms)))
+    return {"block": b.value, "per_tile": p.value,
+            "persistent": bool(q.value), "n_candidates": n.value,
             "best_ms": ms.value}
 
 

@@ -416,21 +416,23 @@ int dust2_gb300_filter_reorder_times(dust2_gb300_filter* filter, double* ms,
 
 /* The step kernel's launch shape: group tiles of `block` threads
  * (per_tile 0), or one-warp tiles of per_tile (1..32) particles (block
- * 32).  By default (autotune 1) the filter times every candidate shape
- * once, before its first run, on scratch copies of its particles, and
- * keeps the fastest; set_step_shape forces one and turns that off.
+ * 32); one block per tile (persistent 0), or (persistent 1) a grid that
+ * fills the device once and takes tiles from a device work queue.  By default (autotune 1) the filter times every candidate
+ * shape once, before its first run, on scratch copies of its particles,
+ * and keeps the fastest; set_step_shape forces one and turns that off.
  * Results do not depend on the shape.  No counterpart in the reference,
  * whose CPU loop has no launch shape. */
 int dust2_gb300_filter_set_autotune(dust2_gb300_filter* filter,
                                     int32_t enable);
 int dust2_gb300_filter_set_step_shape(dust2_gb300_filter* filter,
-                                      int32_t block, int32_t per_tile);
+                                      int32_t block, int32_t per_tile,
+                                      int32_t persistent);
 /* The shape in use, how many candidates were timed (0 before tuning or
  * when it was skipped) and the chosen candidate's time (ms) for one
  * observation's steps. */
 int dust2_gb300_filter_step_shape(dust2_gb300_filter* filter, int32_t* block,
-                                  int32_t* per_tile, int32_t* n_candidates,
-                                  double* best_ms);
+                                  int32_t* per_tile, int32_t* persistent,
+                                  int32_t* n_candidates, double* best_ms);
 
 /* ---- deterministic likelihood (r/unfilter.hpp, unfilter.hpp) ---------- */
 

@@ -434,7 +434,8 @@ def test_scale_log_weights_hook(port):
 
 def test_step_shapes_give_identical_results(port):
     """Every launch shape of the step kernel (group tiles of 32-256
-    threads, one-warp tiles of 1-16 particles) gives the same
+    threads, one-warp tiles of 1-16 particles, one block per tile or a
+    persistent grid taking tiles from a work queue) gives the same
     log-likelihoods, state and generators, equal to the oracle's; the
     autotuner times the candidates and keeps one of them."""
     gen = d.sir_cases()
@@ -447,8 +448,10 @@ def test_step_shapes_give_identical_results(port):
     cols = {"time": np.repeat(times, 3), "incidence": data.ravel(),
             "group": np.tile(np.arange(1, 4), times.size)}
     results = []
-    for shape in [(32, 0), (64, 0), (128, 0), (256, 0), (32, 1), (32, 3),
-                  (32, 16), None]:
+    for shape in [(32, 0, False), (64, 0, False), (128, 0, False),
+                  (256, 0, False), (32, 1, False), (32, 3, False),
+                  (32, 16, False), (64, 0, True), (256, 0, True),
+                  (32, 2, True), None]:
         obj = d.dust_filter_create(gen, 0, cols, n_particles=npg, dt=0.25,
                                    seed=21)
         if shape is not None:
@@ -459,10 +462,11 @@ def test_step_shapes_give_identical_results(port):
         rng = np.frombuffer(d.dust_likelihood_rng_state(obj), dtype="<u8")
         info = d.dust_likelihood_step_shape(obj)
         if shape is not None:
-            assert (info["block"], info["per_tile"]) == shape
+            assert (info["block"], info["per_tile"],
+                    info["persistent"]) == shape
             assert info["n_candidates"] == 0
         else:
-            assert info["n_candidates"] >= 4  # tuned among the candidates
+            assert info["n_candidates"] >= 8  # tuned among the candidates
             assert info["best_ms"] > 0
         results.append((ll, state, rng))
     flat = np.concatenate([gen.pack_pars(p) for p in plist])
