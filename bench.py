@@ -590,8 +590,9 @@ def serve_workload(simulate, steps, packer=None):
     return w
 
 
-def serve_config(args, w):
-    """The config object of both arms of the serving benchmark."""
+def serve_config(args, w, world=1):
+    """The config object of both arms of the serving benchmark (with
+    `world` replicas, one server per GPU)."""
     clients = w["clients"]
     return {"workload": "serve_seir", "system": "seir_age (16 ages, 96 "
             "states, dt 0.25, negative-binomial compare)",
@@ -605,7 +606,7 @@ def serve_config(args, w):
             "hbm_budget_bytes": args.hbm_budget,
             "l2": "not flushed: a continuous request stream; each "
                   "request's state (0.4-50 MB) is resident between requests",
-            "parallelism": "1 GPU, one server"}
+            "parallelism": f"replicas x{world}, one server per GPU"}
 
 
 def seir_device_rate(simulate, n_obs=365):
@@ -647,11 +648,19 @@ def serve_arm(args, rank, world, local):
     is submit to result on both arms, and both include host parameters
     in and host log-likelihoods out.  The plain arm's per-request rate is
     compared with the device's full rate on this system (the batched SEIR
-    filter) to bound what any batching can gain over it."""
+    filter) to bound what any batching can gain over it.
+
+    Under torchrun every rank is an independent replica (its own server
+    and plain executor on its own GPU, the same request stream): both
+    arms start after a barrier, their times are the slowest rank's, and
+    rates count the requests of all ranks."""
     import queue
 
     import torch
+    import torch.distributed as dist
     torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
     import __graft_entry__
     __graft_entry__.build()
     import dust2_gb300 as d
@@ -683,6 +692,8 @@ def serve_arm(args, rank, world, local):
     served_lat = []
     lock = threading.Lock()
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     t0 = time.perf_counter()
     t_end = [t0] * C
 
@@ -707,9 +718,9 @@ def serve_arm(args, rank, world, local):
         th.start()
     for th in threads:
         th.join()
-    served_s = max(t_end) - t0
+    served_s = max_over_ranks(max(t_end) - t0, world, "cuda")
     st = server.stats()
-    served_value = total_ps / served_s
+    served_value = world * total_ps / served_s
     step_ms = st["step_kernel_ms"] - st0["step_kernel_ms"]
     launches = int(st["kernel_launches"] - st0["kernel_launches"])
     server_info = {k: st[k] for k in ("device_steps", "requests_done",
@@ -738,6 +749,8 @@ def serve_arm(args, rank, world, local):
     todo = queue.Queue()
     n_requests = sum(counts)
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     t0 = time.perf_counter()
     t_end = [t0] * C
 
@@ -777,9 +790,9 @@ def serve_arm(args, rank, world, local):
     for th in threads:
         th.join()
     ex.join()
-    plain_s = max(t_end) - t0
+    plain_s = max_over_ranks(max(t_end) - t0, world, "cuda")
     clock_info = clocks.stop()
-    plain_value = total_ps / plain_s
+    plain_value = world * total_ps / plain_s
     same = all(np.array_equal(np.array(a, dtype=float),
                               np.array(b, dtype=float))
                for a, b in zip(served_ll, plain_ll))
@@ -800,13 +813,13 @@ def serve_arm(args, rank, world, local):
     n_par = gen.n_pars
     line = {
         "metric": SERVE_METRIC,
-        "value": served_value, "unit": "particle-steps/s", "n_gpus": 1,
+        "value": served_value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": served_s * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (simulated by the model, seeded)",
-        "config": serve_config(args, w),
+        "config": serve_config(args, w, world),
         "latency_s": {"served": {"p50": percentile(served_lat, 50),
                                  "p99": percentile(served_lat, 99)},
                       "plain": {"p50": percentile(plain_lat, 50),
@@ -857,9 +870,12 @@ def serve_arm(args, rank, world, local):
             "flops_basis": "executed FP64 ops per particle-step of the "
                            "SEIR step kernel (ncu SASS dadd+dmul+2*dfma)"},
     }
-    if not args.no_cpu_baseline:
+    if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = serve_cpu_baseline(w, args.cpu_seconds)
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def ode_alloc(w, seed=1):
@@ -1061,7 +1077,7 @@ def reference_arm(args, rank, world):
         def one():
             return serve_cpu_run(w, picks, threads)
         metric = SERVE_METRIC
-        config = serve_config(args, w)
+        config = serve_config(args, w, world)
     else:
         w = build_workload(args.workload, oracle_simulate(),
                            packer=pyoracle.pack_pars)
@@ -1185,8 +1201,7 @@ def main():
     if args.impl == "reference":
         reference_arm(args, rank, world)
     elif args.workload == "serve_seir":
-        if rank == 0:
-            serve_arm(args, rank, world, local)
+        serve_arm(args, rank, world, local)
     elif args.workload == "ode_batched":
         if rank == 0:
             ode_arm(args, rank, world, local)
