@@ -254,158 +254,6 @@ DUST2_HD double binomial(rng_state& rng, double n, const binomial_prob& b) {
   return b.flip ? n - x : x;
 }
 
-// K binomial draws out[j] ~ Bin(n[j], prob[j]) taken in order from one
-// stream, returning exactly what K calls binomial(rng, n[j], prob[j])
-// return and consuming the same uniforms (errors are recorded in the
-// same order), with the draws' loops merged into one.
-//
-// Why: on the GPU the lanes of a warp are different particles, and each
-// warp instruction costs its FP64 unit the same whether one lane or 32
-// are active.  Drawn one at a time, every draw costs the warp its
-// slowest lane's BINV search length or BTRS attempt count.  Here the
-// set-up of all K draws comes first (the same expressions as
-// binomial()), then one loop in which each lane works through its own
-// sequence of BINV search steps and BTRS attempts, moving to its next
-// draw as soon as the current one is accepted: the warp's loop count is
-// its slowest lane's total over the K draws rather than the sum of the
-// per-draw maxima.  (The lanes that are in a BINV step and those in a
-// BTRS attempt at the same iteration still run both bodies.)
-template <int K>
-DUST2_SAMPLER void binomial_sequence(rng_state& rng, const double* n,
-                                     const binomial_prob* prob,
-                                     double* out) {
-  // per draw: 0 done, 1 BINV, 2 BTRS, 3 invalid arguments
-  int kind[K];
-  double c0[K], c1[K], c2[K], c3[K], c4[K], c5[K];
-  for (int j = 0; j < K; ++j) {
-    const binomial_prob& b = prob[j];
-    const double nj = n[j];
-    const std::uint64_t nb = math::bits_of(nj);
-    kind[j] = 0;
-    if (!binomial_n_ok(nb) || !b.valid) {
-      kind[j] = 3;
-    } else if (rng.deterministic) {
-      out[j] = nj * b.p;
-    } else if ((nb << 1) == 0 || (b.bits << 1) == 0) {
-      out[j] = 0;
-    } else if (b.bits == BITS_ONE) {
-      out[j] = nj;
-    } else if (math::bits_of(nj * b.pp) < BITS_TEN) {
-      kind[j] = 1;
-      c0[j] = (nj + 1.0) * b.s;          // a
-      c1[j] = math::exp(nj * b.logq);    // q^n
-    } else {
-      kind[j] = 2;
-      const double spq = std::sqrt(nj * b.pp * b.q);
-      const double bb = 1.15 + 2.53 * spq;
-      c0[j] = spq;
-      c1[j] = bb;
-      c2[j] = -0.0873 + 0.0248 * bb + 0.01 * b.pp;  // a
-      c3[j] = nj * b.pp + 0.5;                       // c
-      c4[j] = math::rcp(bb);                         // 1 / b
-      c5[j] = 0.92 - 4.2 * c4[j];                    // v_r
-    }
-  }
-  int j = 0;
-  while (j < K && kind[j] == 0) {
-    ++j;
-  }
-  // state of the current draw
-  int tries = 0;           // BINV restarts or BTRS attempts so far
-  bool fresh = true;       // BINV: take a new uniform
-  double u = 0, r = 0;
-  int x = 0;
-  bool have_setup = false;
-  double alpha = 0, m = 0, h = 0;
-  auto finish = [&](double value) {
-    const binomial_prob& b = prob[j];
-    out[j] = b.flip ? n[j] - value : value;
-    ++j;
-    while (j < K && kind[j] == 0) {
-      ++j;
-    }
-    tries = 0;
-    fresh = true;
-    have_setup = false;
-  };
-  while (j < K) {
-    const int kd = kind[j];
-    if (kd == 3) {
-      set_error(rng, ERR_BINOMIAL_INVALID, n[j], prob[j].p);
-      out[j] = math::quiet_nan();
-      ++j;
-      while (j < K && kind[j] == 0) {
-        ++j;
-      }
-      continue;
-    }
-    // a draw that has used up its restarts or attempts is an error (as
-    // in binomial_inversion and binomial_btrs, which see the probability
-    // after symmetry); the NaN stays NaN under the symmetry
-    if (tries >= MAX_REJECTION_ATTEMPTS && (kd == 2 || fresh)) {
-      set_error(rng, ERR_BINOMIAL_INVALID, n[j], prob[j].pp);
-      finish(math::quiet_nan());
-      continue;
-    }
-    if (kd == 1) {
-      // one step of the inversion search (binomial_inversion)
-      if (fresh) {
-        r = c1[j];
-        u = random_real(rng);
-        x = 0;
-        fresh = false;
-        ++tries;
-      }
-      if (math::gt_nonneg(u, r)) {
-        u = u - r;
-        x = x + 1;
-        r = r * (c0[j] * math::recip_int(x) - prob[j].s);
-        if (x > BINV_MAX_X) {
-          fresh = true;
-        }
-      } else {
-        finish(static_cast<double>(x));
-      }
-    } else {
-      // one attempt of BTRS (binomial_btrs)
-      ++tries;
-      const double a = c2[j];
-      const double bb = c1[j];
-      const double inv_b = c4[j];
-      const double uu = random_real(rng) - 0.5;
-      double v = random_real(rng);
-      const double us = 0.5 - math::abs_bits(uu);
-      if (math::bits_of(us) == 0) {
-        continue;
-      }
-      const double inv_us = math::rcp(us);
-      const double k = std::floor((2.0 * a * inv_us + bb) * uu + c3[j]);
-      if (math::le_nonneg(0.07, us) && math::le_nonneg(v, c5[j])) {
-        finish(k);
-        continue;
-      }
-      const std::int64_t k_bits = static_cast<std::int64_t>(math::bits_of(k));
-      const double nj = n[j];
-      if (k_bits < 0 ||
-          k_bits > static_cast<std::int64_t>(math::bits_of(nj))) {
-        continue;
-      }
-      const double pp = prob[j].pp;
-      if (!have_setup) {
-        alpha = (2.83 + 5.1 * inv_b) * c0[j];
-        m = std::floor((nj + 1.0) * pp);
-        h = math::log_factorial(m) + math::log_factorial(nj - m);
-        have_setup = true;
-      }
-      v = math::log(v * alpha * math::rcp(a * inv_us * inv_us + bb));
-      if (v <= h - math::log_factorial(k) - math::log_factorial(nj - k) +
-          (k - m) * prob[j].lpq) {
-        finish(k);
-      }
-    }
-  }
-}
-
 DUST2_HD double poisson_knuth(rng_state& rng, double lambda) {
   const double enlam = math::exp(-lambda);  // > 0 for lambda < 10
   double prod = 1.0;

@@ -31,8 +31,6 @@ struct seir_age {
   // KB per SM) 107.7M -- occupancy hides the FP64 pipe's latency better
   // than shared memory saves local-memory traffic.
   static constexpr int min_blocks_per_sm = 4;
-  // ages whose draws share one merged-loop sampler call (a divisor of 16)
-  static constexpr int batch_ages = 4;
   using real_type = double;
   using rng_state_type = random::rng_state;
   static constexpr int n_age = 16;
@@ -185,44 +183,24 @@ struct seir_age {
     // the same two probabilities serve every age: prepare them once
     const auto b_EI = random::binomial_prepare(p_EI);
     const auto b_IR = random::binomial_prepare(p_IR);
-    // draws per age, in this order: n_SE, n_EI, n_IR.  Given the state at
-    // the start of the step, all of them are known before any is drawn,
-    // so the draws of `batch_ages` ages at a time go to one merged-loop
-    // sampler, which returns what the calls one at a time would.
-    constexpr int K = 3 * batch_ages;
+    // one age per iteration, not unrolled: the body holds three samplers
 #pragma unroll 1
-    for (int a0 = 0; a0 < n_age; a0 += batch_ages) {
-      real_type nn[K];
-      random::binomial_prob pr[K];
-      real_type drawn[K];
-      for (int i = 0; i < batch_ages; ++i) {
-        const int a = a0 + i;
-        real_type acc = 0;
-        for (int b = 0; b < n_age; ++b) {
-          acc = std::fma(shared.contact[a][b], x[b], acc);
-        }
-        const real_type lambda = shared.beta * acc;
-        const real_type p_SE = 1 - math::exp(-lambda * dt);
-        nn[3 * i] = S[a];
-        pr[3 * i] = random::binomial_prepare(p_SE);
-        nn[3 * i + 1] = E[a];
-        pr[3 * i + 1] = b_EI;
-        nn[3 * i + 2] = I[a];
-        pr[3 * i + 2] = b_IR;
+    for (int a = 0; a < n_age; ++a) {
+      real_type acc = 0;
+      for (int b = 0; b < n_age; ++b) {
+        acc = std::fma(shared.contact[a][b], x[b], acc);
       }
-      random::binomial_sequence<K>(rng_state, nn, pr, drawn);
-      for (int i = 0; i < batch_ages; ++i) {
-        const int a = a0 + i;
-        const real_type n_SE = drawn[3 * i];
-        const real_type n_EI = drawn[3 * i + 1];
-        const real_type n_IR = drawn[3 * i + 2];
-        state_next[a] = S[a] - n_SE;
-        state_next[n_age + a] = E[a] + n_SE - n_EI;
-        state_next[2 * n_age + a] = I[a] + n_EI - n_IR;
-        state_next[3 * n_age + a] = R[a] + n_IR;
-        state_next[4 * n_age + a] = cum[a] + n_EI;
-        state_next[5 * n_age + a] = inc[a] + n_EI;
-      }
+      const real_type lambda = shared.beta * acc;
+      const real_type p_SE = 1 - math::exp(-lambda * dt);
+      const real_type n_SE = random::binomial(rng_state, S[a], p_SE);
+      const real_type n_EI = random::binomial(rng_state, E[a], b_EI);
+      const real_type n_IR = random::binomial(rng_state, I[a], b_IR);
+      state_next[a] = S[a] - n_SE;
+      state_next[n_age + a] = E[a] + n_SE - n_EI;
+      state_next[2 * n_age + a] = I[a] + n_EI - n_IR;
+      state_next[3 * n_age + a] = R[a] + n_IR;
+      state_next[4 * n_age + a] = cum[a] + n_EI;
+      state_next[5 * n_age + a] = inc[a] + n_EI;
     }
   }
 

@@ -1529,48 +1529,4 @@ void oracle_rng_streams(uint64_t seed, int n, uint64_t* out) {
   }
 }
 
-// Binomial draws in batches of k (1, 3, 12 or 48) from one stream:
-// merged != 0 through binomial_sequence<k>, else one binomial() call per
-// draw (probabilities prepared the same way).  Checks that the merged
-// loops return the same draws, errors and stream state.
-int oracle_binomial_batches(int merged, int k, int n_batches,
-                            const double* n, const double* p,
-                            const uint64_t* rng, int deterministic,
-                            double* out, uint64_t* rng_out, double* err) {
-  auto r = make_rng(rng, 1, deterministic != 0)[0];
-  auto run = [&](auto kk) {
-    constexpr int K = decltype(kk)::value;
-    for (int i = 0; i < n_batches; ++i) {
-      const double* nb = n + static_cast<size_t>(i) * K;
-      const double* pb = p + static_cast<size_t>(i) * K;
-      double* ob = out + static_cast<size_t>(i) * K;
-      dust2gpu::random::binomial_prob prob[K];
-      for (int j = 0; j < K; ++j) {
-        prob[j] = dust2gpu::random::binomial_prepare(pb[j]);
-      }
-      if (merged) {
-        dust2gpu::random::binomial_sequence<K>(r, nb, prob, ob);
-      } else {
-        for (int j = 0; j < K; ++j) {
-          ob[j] = dust2gpu::random::binomial(r, nb[j], prob[j]);
-        }
-      }
-    }
-  };
-  switch (k) {
-  case 1: run(std::integral_constant<int, 1>{}); break;
-  case 3: run(std::integral_constant<int, 3>{}); break;
-  case 12: run(std::integral_constant<int, 12>{}); break;
-  case 48: run(std::integral_constant<int, 48>{}); break;
-  default: return 1;
-  }
-  for (int w = 0; w < 4; ++w) {
-    rng_out[w] = r.state[w];
-  }
-  err[0] = r.err;
-  err[1] = r.err_v0;
-  err[2] = r.err_v1;
-  return 0;
-}
-
 }  // extern "C"
