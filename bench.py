@@ -921,25 +921,30 @@ def ode_cpu_baseline(w, target_seconds):
             "seconds": t, "instances": n}
 
 
-def ode_config(w):
+def ode_config(w, world=1):
     """The config object of both arms of the dopri5 benchmark."""
     return {"workload": "ode_batched", "system": "sirode",
             "instances": w["n_groups"], "outputs": int(w["times"].size),
             "rtol": 1e-6, "atol": 1e-6,
             "l2": "flushed (256 MB write) between timed steps; outputs "
                   f"{w['n_groups'] * w['times'].size * 40 / 1e9:.1f} GB",
-            "parallelism": "1 GPU"}
+            "parallelism": f"replicas x{world}"}
 
 
 def ode_arm(args, rank, world, local):
     """Batched dopri5: 262,144 sirode instances integrated 0..200 with
     output at every integer time (rtol = atol = 1e-6).  A step of the
     benchmark is one simulate of every instance from t = 0; the metric
-    counts attempted dopri5 steps (accepted + rejected) per second."""
+    counts attempted dopri5 steps (accepted + rejected) per second.
+    Under torchrun every rank integrates its own copy (replicas): timed
+    steps start after a barrier and the slowest rank's time counts."""
     import ctypes
 
     import torch
+    import torch.distributed as dist
     torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
     import __graft_entry__
     __graft_entry__.build()
     from dust2_gb300 import _lib, workloads
@@ -983,6 +988,8 @@ def ode_arm(args, rank, world, local):
     clocks.start()
     time.sleep(0.5)
     elapsed = []
+    if world > 1:
+        dist.barrier()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
@@ -997,7 +1004,7 @@ def ode_arm(args, rank, world, local):
         torch.cuda.synchronize()
         elapsed.append(e0.elapsed_time(e1))
     clock_info = clocks.stop()
-    ms = float(np.mean(elapsed))
+    ms = max_over_ranks(float(np.mean(elapsed)), world, "cuda")
     # the caller's output buffer: pinned host memory, as the timing
     # contract's host<->device copies are
     host_t = torch.empty(n_out, dtype=torch.float64, pin_memory=True)
@@ -1012,22 +1019,22 @@ def ode_arm(args, rank, world, local):
         t0 = time.perf_counter()
         run_once(device=False, host_out=host)
         e2e.append(time.perf_counter() - t0)
-    e2e_s = float(np.mean(e2e))
+    e2e_s = max_over_ranks(float(np.mean(e2e)), world, "cuda")
     peak = fp64_peak_tflops()
     ops = FP64_OPS_PER_PARTICLE_STEP.get("ode_batched")
     achieved = None if ops is None else ops * steps / (ms * 1e-3) / 1e12
     _lib.check(lib.dust2_gb300_system_free(h))
     line = {
-        "metric": "dopri5 steps/s", "value": steps / (ms * 1e-3),
-        "unit": "dopri5 steps/s", "n_gpus": 1, "steps": args.steps,
+        "metric": "dopri5 steps/s", "value": world * steps / (ms * 1e-3),
+        "unit": "dopri5 steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded parameters)",
-        "config": ode_config(w),
+        "config": ode_config(w, world),
         "dopri5": {"steps_per_step": steps, "accepted": int(na.sum()),
                    "rejected": int(nr.sum()),
                    "steps_per_instance": [int(ns.min()), int(ns.max())]},
-        "e2e": {"value": steps / e2e_s, "unit": "dopri5 steps/s",
+        "e2e": {"value": world * steps / e2e_s, "unit": "dopri5 steps/s",
                 "h2d_bytes_per_step": times.size * 8,
                 "d2h_bytes_per_step": n_out * 8, "seconds_per_step": e2e_s},
         "gpu_launches": 2 * args.steps,
@@ -1041,9 +1048,12 @@ def ode_arm(args, rank, world, local):
                      "flops_basis": "executed FP64 ops per attempted "
                                     "dopri5 step (ncu SASS)"},
     }
-    if not args.no_cpu_baseline:
+    if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = ode_cpu_baseline(w, args.cpu_seconds)
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 def reference_arm(args, rank, world):
@@ -1072,7 +1082,7 @@ def reference_arm(args, rank, world):
         def one():
             return ode_cpu(w, n_inst, threads)
         metric, unit = "dopri5 steps/s", "dopri5 steps/s"
-        config = ode_config(w)
+        config = ode_config(w, world)
     elif args.workload == "serve_seir":
         w = serve_workload(oracle_simulate(), args.steps,
                            packer=pyoracle.pack_pars)
@@ -1207,8 +1217,7 @@ def main():
     elif args.workload == "serve_seir":
         serve_arm(args, rank, world, local)
     elif args.workload == "ode_batched":
-        if rank == 0:
-            ode_arm(args, rank, world, local)
+        ode_arm(args, rank, world, local)
     else:
         gpu_arm(args, rank, world, local)
 
