@@ -75,7 +75,7 @@ DUST2_SAMPLER double binomial_inversion(rng_state& rng, double n, double p,
     while (math::gt_nonneg(u, r)) {
       u = u - r;
       x = x + 1;
-      r = r * (a * math::recip_int(x) - s);
+      r = r * std::fma(a, math::recip_int(x), -s);
       if (x > BINV_MAX_X) {
         break;
       }
@@ -110,11 +110,12 @@ template <typename LPQ>
 DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
                               const LPQ& lpq_of) {
   const double spq = std::sqrt(n * p * q);
-  const double b = 1.15 + 2.53 * spq;
-  const double a = -0.0873 + 0.0248 * b + 0.01 * p;
-  const double c = n * p + 0.5;
+  const double b = std::fma(2.53, spq, 1.15);
+  const double a = std::fma(0.01, p, std::fma(0.0248, b, -0.0873));
+  const double a2 = 2.0 * a;
+  const double c = std::fma(n, p, 0.5);
   const double inv_b = math::rcp(b);
-  const double v_r = 0.92 - 4.2 * inv_b;
+  const double v_r = std::fma(-4.2, inv_b, 0.92);
   const std::int64_t n_bits = static_cast<std::int64_t>(math::bits_of(n));
   bool have_setup = false;
   double alpha = 0, lpq = 0, m = 0, h = 0;
@@ -126,7 +127,7 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
       continue;
     }
     const double inv_us = math::rcp(us);
-    const double k = std::floor((2.0 * a * inv_us + b) * u + c);
+    const double k = std::floor(std::fma(std::fma(a2, inv_us, b), u, c));
     if (math::le_nonneg(0.07, us) && math::le_nonneg(v, v_r)) {
       return k;
     }
@@ -137,15 +138,15 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
       continue;
     }
     if (!have_setup) {
-      alpha = (2.83 + 5.1 * inv_b) * spq;
+      alpha = std::fma(5.1, inv_b, 2.83) * spq;
       lpq = lpq_of();
       m = std::floor((n + 1.0) * p);
       h = math::log_factorial(m) + math::log_factorial(n - m);
       have_setup = true;
     }
-    v = math::log(v * alpha * math::rcp(a * inv_us * inv_us + b));
-    if (v <= h - math::log_factorial(k) - math::log_factorial(n - k) +
-        (k - m) * lpq) {
+    v = math::log(v * alpha * math::rcp(std::fma(a * inv_us, inv_us, b)));
+    if (v <= std::fma(k - m, lpq, h - math::log_factorial(k) -
+                      math::log_factorial(n - k))) {
       return k;
     }
   }
@@ -270,9 +271,11 @@ DUST2_HD double poisson_knuth(rng_state& rng, double lambda) {
 // lambda >= 10, so b > 8.9 and vr > 0.4.
 DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   const double slam = std::sqrt(lambda);
-  const double b = 0.931 + 2.53 * slam;
-  const double a = -0.059 + 0.02483 * b;
-  const double vr = 0.9277 - 3.6224 * math::rcp(b - 2.0);
+  const double b = std::fma(2.53, slam, 0.931);
+  const double a = std::fma(0.02483, b, -0.059);
+  const double a2 = 2.0 * a;
+  const double c = lambda + 0.43;
+  const double vr = std::fma(-3.6224, math::rcp(b - 2.0), 0.9277);
   bool have_setup = false;
   double log_invalpha = 0, loglam = 0;
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
@@ -283,7 +286,7 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
       continue;
     }
     const double inv_us = math::rcp(us);
-    const double k = std::floor((2.0 * a * inv_us + b) * u + lambda + 0.43);
+    const double k = std::floor(std::fma(std::fma(a2, inv_us, b), u, c));
     if (math::le_nonneg(0.07, us) && math::le_nonneg(v, vr)) {
       return k;
     }
@@ -293,12 +296,13 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
       continue;
     }
     if (!have_setup) {
-      log_invalpha = math::log(1.1239 + 1.1328 * math::rcp(b - 3.4));
+      log_invalpha = math::log(std::fma(1.1328, math::rcp(b - 3.4), 1.1239));
       loglam = math::log(lambda);
       have_setup = true;
     }
-    if (math::log(v) + log_invalpha - math::log(a * inv_us * inv_us + b) <=
-        -lambda + k * loglam - math::log_factorial(k)) {
+    if (math::log(v) + log_invalpha -
+        math::log(std::fma(a * inv_us, inv_us, b)) <=
+        std::fma(k, loglam, -lambda) - math::log_factorial(k)) {
       return k;
     }
   }

@@ -11,12 +11,14 @@ draws themselves must agree, value for value along whole streams, for
 arguments in every branch: inversion (BINV, Kachitvichyanukul & Schmeiser
 1988) and transformed rejection with squeeze (BTRS, Hormann 1993) for the
 binomial, with p > 1/2 by symmetry; multiplication of uniforms (Knuth)
-and PTRS (Hormann 1993) for the Poisson.  The two sides round their
-elementary functions differently (within an ulp or two), so a draw could
-differ when a comparison falls within that distance of a boundary; on
-these streams none does."""
+and PTRS (Hormann 1993) for the Poisson.  Multiply-adds that the engine
+fuses are fused here too (rounded once, through exact rationals).  The
+two sides round their elementary functions and reciprocals differently
+(within an ulp or two), so a draw could differ when a comparison falls
+within that distance of a boundary; on these streams none does."""
 
 import math
+from fractions import Fraction
 
 import numpy as np
 import pytest
@@ -25,6 +27,12 @@ import xoshiro
 from oracle import pyoracle
 
 BINV_MAX_X = 110
+
+
+def fma(a, b, c):
+    """a * b + c rounded once (exact rational arithmetic, then the
+    correctly rounded conversion to a double)."""
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
 
 
 def uniform(s):
@@ -43,7 +51,7 @@ def binomial_inversion(s, n, p):
         while u > r:
             u -= r
             x += 1
-            r *= a / x - sr
+            r *= fma(a, 1.0 / x, -sr)
             if x > BINV_MAX_X:
                 break
         if x <= BINV_MAX_X:
@@ -57,27 +65,27 @@ def log_factorial(k):
 def binomial_btrs(s, n, p):
     q = 1.0 - p
     spq = math.sqrt(n * p * q)
-    b = 1.15 + 2.53 * spq
-    a = -0.0873 + 0.0248 * b + 0.01 * p
-    c = n * p + 0.5
-    v_r = 0.92 - 4.2 / b
+    b = fma(2.53, spq, 1.15)
+    a = fma(0.01, p, fma(0.0248, b, -0.0873))
+    c = fma(n, p, 0.5)
+    v_r = fma(-4.2, 1.0 / b, 0.92)
     while True:
         u = uniform(s) - 0.5
         v = uniform(s)
         us = 0.5 - abs(u)
         if us == 0:
             continue
-        k = math.floor((2.0 * a / us + b) * u + c)
+        k = math.floor(fma(fma(2.0 * a, 1.0 / us, b), u, c))
         if us >= 0.07 and v <= v_r:
             return float(k)
         if k < 0 or k > n:
             continue
-        alpha = (2.83 + 5.1 / b) * spq
+        alpha = fma(5.1, 1.0 / b, 2.83) * spq
         lpq = math.log(p / q)
         m = math.floor((n + 1.0) * p)
         h = log_factorial(m) + log_factorial(n - m)
-        v = math.log(v * alpha / (a / (us * us) + b))
-        if v <= h - log_factorial(k) - log_factorial(n - k) + (k - m) * lpq:
+        v = math.log(v * alpha / fma(a / us, 1.0 / us, b))
+        if v <= fma(k - m, lpq, h - log_factorial(k) - log_factorial(n - k)):
             return float(k)
 
 
@@ -108,23 +116,23 @@ def poisson(s, lam):
                 return float(x)
             x += 1
     slam = math.sqrt(lam)
-    b = 0.931 + 2.53 * slam
-    a = -0.059 + 0.02483 * b
-    vr = 0.9277 - 3.6224 / (b - 2.0)
+    b = fma(2.53, slam, 0.931)
+    a = fma(0.02483, b, -0.059)
+    vr = fma(-3.6224, 1.0 / (b - 2.0), 0.9277)
     while True:
         u = uniform(s) - 0.5
         v = uniform(s)
         us = 0.5 - abs(u)
         if us == 0:
             continue
-        k = math.floor((2.0 * a / us + b) * u + lam + 0.43)
+        k = math.floor(fma(fma(2.0 * a, 1.0 / us, b), u, lam + 0.43))
         if us >= 0.07 and v <= vr:
             return float(k)
         if k < 0 or (us < 0.013 and v > us):
             continue
-        log_invalpha = math.log(1.1239 + 1.1328 / (b - 3.4))
-        if (math.log(v) + log_invalpha - math.log(a / (us * us) + b) <=
-                -lam + k * math.log(lam) - math.lgamma(k + 1.0)):
+        log_invalpha = math.log(fma(1.1328, 1.0 / (b - 3.4), 1.1239))
+        if (math.log(v) + log_invalpha - math.log(fma(a / us, 1.0 / us, b))
+                <= fma(k, math.log(lam), -lam) - math.lgamma(k + 1.0)):
             return float(k)
 
 
