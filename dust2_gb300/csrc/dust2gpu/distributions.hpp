@@ -120,9 +120,9 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
   bool have_setup = false;
   double alpha = 0, lpq = 0, m = 0, h = 0;
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
-    const double u = random_real(rng) - 0.5;
+    double u, us;  // U - 1/2 and 1/2 - |U - 1/2|, us >= +0
+    centered_uniform(rng, &u, &us);
     double v = random_real(rng);
-    const double us = 0.5 - math::abs_bits(u);  // >= +0
     if (math::bits_of(us) == 0) {
       continue;
     }
@@ -279,9 +279,9 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   bool have_setup = false;
   double log_invalpha = 0, loglam = 0;
   for (int attempt = 0; attempt < MAX_REJECTION_ATTEMPTS; ++attempt) {
-    const double u = random_real(rng) - 0.5;
+    double u, us;  // U - 1/2 and 1/2 - |U - 1/2|, us >= +0
+    centered_uniform(rng, &u, &us);
     const double v = random_real(rng);
-    const double us = 0.5 - math::abs_bits(u);  // >= +0
     if (math::bits_of(us) == 0) {
       continue;
     }

@@ -88,6 +88,27 @@ DUST2_HD double random_real(rng_state& s) {
   return math::u53_to_unit(next(s) >> 11);
 }
 
+// For the next uniform U of random_real (U = m 2^-53): u = U - 1/2 and
+// us = 1/2 - |u|.  Both are multiples of 2^-53 smaller than 1, so the
+// FP64 subtractions are exact; here they are assembled from the integer
+// m - 2^52 on the integer pipe, with the same values and signs (U = 1/2
+// gives u = +0; U = 0 gives us = +0).
+DUST2_HD void centered_uniform(rng_state& s, double* u, double* us) {
+  if (s.deterministic) {
+    *u = 0.0;
+    *us = 0.5;
+    return;
+  }
+  const std::uint64_t m = next(s) >> 11;
+  constexpr std::uint64_t half = static_cast<std::uint64_t>(1) << 52;
+  const bool neg = m < half;
+  const std::uint64_t ad = neg ? half - m : m - half;
+  const double mag = math::u53_to_unit(ad);
+  *u = neg ? math::from_bits(math::bits_of(mag) | 0x8000000000000000ull) :
+    mag;
+  *us = math::u53_to_unit(half - ad);
+}
+
 // Advance a stream by 2^128 draws.  The characteristic-polynomial
 // coefficients are the published jump constants for xoshiro256.
 DUST2_HD void jump(std::uint64_t* s) {

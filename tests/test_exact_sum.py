@@ -32,3 +32,24 @@ def test_exact_running_sum_matches_plain_loop(tmp_path):
     # the windows stay few: about one per 128..1024 weights plus the
     # binade crossings
     assert float(fields[5]) < 20
+
+
+def test_centered_uniform_matches_fp64_subtractions(tmp_path):
+    """random::centered_uniform (U - 1/2 and 1/2 - |U - 1/2| assembled on
+    the integer pipe for the BTRS and PTRS attempts) equals the FP64
+    subtractions bit for bit."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "centered_uniform_check"
+    subprocess.run(
+        [cxx, "-O2", "-std=c++17", "-ffp-contract=off",
+         "-I", str(ROOT / "dust2_gb300" / "csrc"),
+         str(ROOT / "tests" / "centered_uniform_check.cpp"), "-o", str(exe)],
+        check=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stdout + res.stderr
+    fields = res.stdout.split()
+    assert fields[:1] == ["cases"] and int(fields[1]) > 5000000
+    assert fields[2] == "bad" and int(fields[3]) == 0
