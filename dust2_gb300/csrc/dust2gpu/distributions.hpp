@@ -127,7 +127,7 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
       continue;
     }
     const double inv_us = math::rcp(us);
-    const double k = std::floor(std::fma(std::fma(a2, inv_us, b), u, c));
+    const double k = math::floor_bits(std::fma(std::fma(a2, inv_us, b), u, c));
     if (math::le_nonneg(0.07, us) && math::le_nonneg(v, v_r)) {
       return k;
     }
@@ -140,7 +140,7 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
     if (!have_setup) {
       alpha = std::fma(5.1, inv_b, 2.83) * spq;
       lpq = lpq_of();
-      m = std::floor((n + 1.0) * p);
+      m = math::floor_bits((n + 1.0) * p);
       h = math::log_factorial(m) + math::log_factorial(n - m);
       have_setup = true;
     }
@@ -286,7 +286,7 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
       continue;
     }
     const double inv_us = math::rcp(us);
-    const double k = std::floor(std::fma(std::fma(a2, inv_us, b), u, c));
+    const double k = math::floor_bits(std::fma(std::fma(a2, inv_us, b), u, c));
     if (math::le_nonneg(0.07, us) && math::le_nonneg(v, vr)) {
       return k;
     }

@@ -183,6 +183,32 @@ DUST2_HD bool le_nonneg(double a, double b) {
   return bits_of(a) <= bits_of(b);
 }
 
+// floor(x) on the integer pipe, the same value as std::floor for every
+// x (including -0, infinities and NaN): the fraction bits are cleared,
+// and a negative x with a fraction moves one unit further from zero (a
+// carry out of the mantissa lands in the exponent, as it should).
+DUST2_HD double floor_bits(double x) {
+  const std::uint64_t u = bits_of(x);
+  const int e = static_cast<int>((u >> 52) & 0x7ff);
+  const bool neg = (u >> 63) != 0;
+  if (e >= 1075) {  // |x| >= 2^52, infinite or NaN: already integral
+    return x;
+  }
+  if (e < 1023) {  // |x| < 1
+    if ((u << 1) == 0 || !neg) {
+      return from_bits(u & 0x8000000000000000ull);  // +-0
+    }
+    return -1.0;
+  }
+  const std::uint64_t unit = static_cast<std::uint64_t>(1) << (1075 - e);
+  const std::uint64_t frac = u & (unit - 1);
+  if (frac == 0) {
+    return x;
+  }
+  const std::uint64_t t = u - frac;  // toward zero
+  return from_bits(neg ? t + unit : t);
+}
+
 // |x| by clearing the sign bit.
 DUST2_HD double abs_bits(double x) {
   return from_bits(bits_of(x) & 0x7fffffffffffffffull);

@@ -1,8 +1,12 @@
 // Checks random::centered_uniform against the FP64 subtractions it
 // replaces (u = U - 1/2, us = 1/2 - |u| for U = random_real), bit for
 // bit, on the edge values of the 53-bit integer behind U and on 5 million
-// random ones.  Prints "cases N bad B".
+// random ones; and math::floor_bits against std::floor on special values,
+// values near integers and powers of two, and random bit patterns.
+// Prints "cases N bad B".
+#include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <random>
 
 #include "dust2gpu/random.hpp"
@@ -38,6 +42,45 @@ int main() {
   }
   for (int i = 0; i < 5000000; ++i) {
     check(g() >> 11);
+  }
+  auto check_floor = [&](double x) {
+    ++cases;
+    if (math::bits_of(math::floor_bits(x)) != math::bits_of(std::floor(x))) {
+      ++bad;
+    }
+  };
+  for (double x : {0.0, -0.0, 0.5, -0.5, 1.0, -1.0, 1.5, -1.5, 2.0, -2.0,
+                   0x1p52, -0x1p52, 0x1p52 + 1, 0x1.fffffffffffffp51,
+                   -0x1.fffffffffffffp51, 0x1.fffffffffffffp-1,
+                   -0x1.fffffffffffffp-1, 0x1p-1074, -0x1p-1074,
+                   1e300, -1e300, HUGE_VAL, -HUGE_VAL}) {
+    check_floor(x);
+  }
+  for (int k = -60; k <= 60; ++k) {
+    const double p2 = std::ldexp(1.0, k);
+    for (double d : {-1.0, 0.0, 1.0}) {
+      const double x = p2 + d * std::ldexp(1.0, k - 52);
+      check_floor(x);
+      check_floor(-x);
+      check_floor(std::nextafter(x, 0.0));
+      check_floor(-std::nextafter(x, 0.0));
+    }
+  }
+  std::uniform_real_distribution<double> wide(-1e6, 1e6);
+  for (int i = 0; i < 2000000; ++i) {
+    check_floor(wide(g));
+    check_floor(std::round(wide(g)));
+    unsigned long long b = g();
+    double x;
+    std::memcpy(&x, &b, 8);
+    if (!std::isnan(x)) {
+      check_floor(x);
+    }
+  }
+  const double nan = std::nan("");
+  ++cases;
+  if (!std::isnan(math::floor_bits(nan))) {
+    ++bad;
   }
   std::printf("cases %ld bad %ld\n", cases, bad);
   return bad != 0;
