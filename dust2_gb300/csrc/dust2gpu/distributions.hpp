@@ -112,7 +112,7 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
   const double spq = std::sqrt(n * p * q);
   const double b = std::fma(2.53, spq, 1.15);
   const double a = std::fma(0.01, p, std::fma(0.0248, b, -0.0873));
-  const double a2 = 2.0 * a;
+  const double a2 = math::twice_normal(a);  // a > 0.08
   const double c = std::fma(n, p, 0.5);
   const double inv_b = math::rcp(b);
   const double v_r = std::fma(-4.2, inv_b, 0.92);
@@ -273,7 +273,7 @@ DUST2_HD double poisson_ptrs(rng_state& rng, double lambda) {
   const double slam = std::sqrt(lambda);
   const double b = std::fma(2.53, slam, 0.931);
   const double a = std::fma(0.02483, b, -0.059);
-  const double a2 = 2.0 * a;
+  const double a2 = math::twice_normal(a);  // a > 0.16
   const double c = lambda + 0.43;
   const double vr = std::fma(-3.6224, math::rcp(b - 2.0), 0.9277);
   bool have_setup = false;

@@ -209,6 +209,12 @@ DUST2_HD double floor_bits(double x) {
   return from_bits(neg ? t + unit : t);
 }
 
+// 2 x for a normal x whose double is also normal (an exponent
+// increment: the same value as the exact FP64 product).
+DUST2_HD double twice_normal(double x) {
+  return from_bits(bits_of(x) + (static_cast<std::uint64_t>(1) << 52));
+}
+
 // |x| by clearing the sign bit.
 DUST2_HD double abs_bits(double x) {
   return from_bits(bits_of(x) & 0x7fffffffffffffffull);

@@ -1,8 +1,9 @@
 // Checks random::centered_uniform against the FP64 subtractions it
 // replaces (u = U - 1/2, us = 1/2 - |u| for U = random_real), bit for
 // bit, on the edge values of the 53-bit integer behind U and on 5 million
-// random ones; and math::floor_bits against std::floor on special values,
-// values near integers and powers of two, and random bit patterns.
+// random ones; math::floor_bits against std::floor on special values,
+// values near integers and powers of two, and random bit patterns; and
+// math::twice_normal against 2 x.
 // Prints "cases N bad B".
 #include <cmath>
 #include <cstdio>
@@ -75,6 +76,15 @@ int main() {
     std::memcpy(&x, &b, 8);
     if (!std::isnan(x)) {
       check_floor(x);
+    }
+  }
+  // the exact doubling used for BTRS's and PTRS's 2a
+  for (int i = 0; i < 1000000; ++i) {
+    const double x = std::ldexp(1.0 + (g() >> 12) * 0x1p-52,
+                                static_cast<int>(g() % 2000) - 1000);
+    ++cases;
+    if (math::bits_of(math::twice_normal(x)) != math::bits_of(2.0 * x)) {
+      ++bad;
     }
   }
   const double nan = std::nan("");
