@@ -170,6 +170,10 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=12.0,
                    help="target CPU time of the bounded CPU sample")
+    p.add_argument("--step-shape", default=None,
+                   help="filter workloads: force the step kernel's launch "
+                        "shape, block,per_tile,persistent (e.g. 64,0,0), "
+                        "instead of the autotuner's choice")
     return p.parse_args()
 
 
@@ -407,6 +411,9 @@ def gpu_arm(args, rank, world, local):
                                n_particles=npg if len(npg) > 1 else npg[0],
                                dt=w["dt"], seed=w["seed"])
     plist = w["plist"] if len(npg) > 1 else w["plist"][0]
+    if args.step_shape:
+        b, pt, pe = (int(x) for x in args.step_shape.split(","))
+        d.dust_likelihood_set_step_shape(obj, b, pt, bool(pe))
     d.dust_likelihood_run(obj, plist)  # allocate and initialise
     lib = _lib.lib()
     h = obj.ptr

@@ -1064,13 +1064,14 @@ public:
     v.any_error = any.data();
     const int run_tiles = S.n_run_tiles();
     k_initial<T><<<run_tiles, L.tile_size, 0, s>>>(v, nullptr, time_start_);
-    // part of the way in: half the schedule's steps, at most 100
+    // part of the way in: half the schedule's steps, at most 400 (the
+    // cost of a step depends on the state, and early states are cheap)
     const std::size_t mid = schedule_.size() / 2;
     int steps = 0;
     for (std::size_t i = 0; i < mid; ++i) {
       steps += schedule_[i].n_steps;
     }
-    steps = std::min(steps, 100);
+    steps = std::min(steps, 400);
     if (steps > 0) {
       k_run<T><<<run_tiles, L.tile_size, 0, s>>>(v, time_start_, S.dt(),
                                                  steps);
