@@ -73,7 +73,7 @@ DUST2_SAMPLER double binomial_inversion(rng_state& rng, double n, double p,
     double u = random_real(rng);
     int x = 0;
     while (math::gt_nonneg(u, r)) {
-      u = math::sub_gt_nonneg(u, r);  // u - r, on the integer pipe
+      u = u - r;
       x = x + 1;
       r = r * std::fma(a, math::recip_int(x), -s);
       if (x > BINV_MAX_X) {

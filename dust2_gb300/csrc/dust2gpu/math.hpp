@@ -306,58 +306,6 @@ DUST2_HD int clz64(std::uint64_t v) {
 }
 #endif
 
-// u - r for finite u > r >= 0, rounded to nearest even, on the integer
-// pipe: the same bits as the FP64 subtraction (subnormals included).
-// The significands, with 8 guard bits, are aligned on u's exponent, the
-// bits shifted out of r are kept as a sticky bit, and the difference is
-// normalised (down to the subnormal range) and rounded once.
-DUST2_HD double sub_gt_nonneg(double u, double r) {
-  const std::uint64_t bu = bits_of(u);
-  const std::uint64_t br = bits_of(r);
-  if (br == 0) {
-    return u;
-  }
-  constexpr std::uint64_t MANT = 0x000fffffffffffffull;
-  constexpr std::uint64_t HIDDEN = static_cast<std::uint64_t>(1) << 52;
-  const int eu = static_cast<int>(bu >> 52);
-  const int er = static_cast<int>(br >> 52);
-  const std::uint64_t a = ((bu & MANT) | (eu != 0 ? HIDDEN : 0)) << 8;
-  const std::uint64_t b = ((br & MANT) | (er != 0 ? HIDDEN : 0)) << 8;
-  const int e_u = eu != 0 ? eu : 1;
-  const int d = e_u - (er != 0 ? er : 1);
-  std::uint64_t shifted, sticky;
-  if (d >= 64) {
-    shifted = 0;
-    sticky = 1;
-  } else {
-    shifted = b >> d;
-    sticky = (b & ((static_cast<std::uint64_t>(1) << d) - 1)) != 0 ? 1 : 0;
-  }
-  // the exact difference lies in (diff, diff + 1) when sticky is set;
-  // keeping the sticky bit in the lowest place rounds it correctly
-  std::uint64_t diff = (a - shifted - sticky) | sticky;
-  int lz = clz64(diff) - 3;  // leading one to bit 60
-  int e = e_u - lz;
-  if (e < 1) {  // subnormal result: stop at the smallest exponent
-    lz -= 1 - e;
-    e = 0;
-  }
-  diff <<= lz;
-  const std::uint64_t low = diff & 0xff;
-  std::uint64_t m = diff >> 8;
-  if (low > 0x80 || (low == 0x80 && (m & 1) != 0)) {
-    m += 1;
-  }
-  if (e == 0) {
-    return from_bits(m);  // a carry into bit 52 is the smallest normal
-  }
-  if ((m >> 53) != 0) {
-    m >>= 1;
-    e += 1;
-  }
-  return from_bits((static_cast<std::uint64_t>(e) << 52) | (m & MANT));
-}
-
 // v * 2^-scale for a non-zero unsigned 128-bit v, rounded to 53 bits
 // (ties away from zero) with the given sign; the result must be normal.
 DUST2_HD double u128_to_double(u128 v, int scale, bool negative) {

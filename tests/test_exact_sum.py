@@ -37,9 +37,8 @@ def test_exact_running_sum_matches_plain_loop(tmp_path):
 def test_integer_pipe_replacements_match_fp64(tmp_path):
     """The FP64 operations of the samplers done on the integer pipe give
     the FP64 bits: random::centered_uniform (U - 1/2 and 1/2 - |U - 1/2|
-    of the BTRS and PTRS attempts), math::floor_bits (std::floor),
-    math::twice_normal (2 x) and math::sub_gt_nonneg (u - r of the BINV
-    search)."""
+    of the BTRS and PTRS attempts), math::floor_bits (std::floor) and
+    math::twice_normal (2 x)."""
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("g++ not available")
@@ -53,5 +52,5 @@ def test_integer_pipe_replacements_match_fp64(tmp_path):
                          timeout=300)
     assert res.returncode == 0, res.stdout + res.stderr
     fields = res.stdout.split()
-    assert fields[:1] == ["cases"] and int(fields[1]) > 19000000
+    assert fields[:1] == ["cases"] and int(fields[1]) > 12000000
     assert fields[2] == "bad" and int(fields[3]) == 0
