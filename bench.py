@@ -93,6 +93,34 @@ def formulation_roofline(workload, units_per_s, peak_tflops):
                      "exp/log in FP64 (ncu, earlier build)"}
 
 
+# The algorithmic basis: FP64 operations per particle-step of the step +
+# compare work counted by running the systems and the binomial sampler
+# over an operation-counting real type (oracle/opcount: +, -, *, / and
+# sqrt one flop each, a fused multiply-add two; exp, log, log k! and
+# lgamma counted as calls, not flops), on a sample of each batched
+# workload whose log-likelihoods equal the oracle port's bit for bit
+# (`python -m oracle.opcount.count`: batched SIR groups 1-8, all
+# particles; batched SEIR groups 1-4 at 1024 particles; all observations).
+FP64_ALGORITHMIC_OPS = {"sir_batched": 59.95, "seir_batched": 1738.7}
+ALGORITHMIC_CALLS = {
+    "sir_batched": {"exp": 1.66, "log": 1.28, "log_factorial": 1.72,
+                    "lgamma": 0.25},
+    "seir_batched": {"exp": 44.4, "log": 26.7, "log_factorial": 35.2,
+                     "lgamma": 0.75}}
+
+
+def algorithmic_roofline(workload, units_per_s, peak_tflops):
+    ops = FP64_ALGORITHMIC_OPS.get(workload)
+    if ops is None or not units_per_s:
+        return None
+    achieved = ops * units_per_s / 1e12
+    return {"flops_per_unit": ops, "achieved": achieved,
+            "frac": achieved / peak_tflops, "unit": "TFLOP/s",
+            "calls_per_unit": ALGORITHMIC_CALLS[workload],
+            "basis": "FP64 operations of the model and samplers counted "
+                     "by an operation-counting real type (oracle/opcount)"}
+
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
 # same kernel, from ncu captures (SIR and dopri5: whole runs; SEIR: one
 # launch at observation 200 of the current build, which keeps the state
@@ -533,6 +561,8 @@ def gpu_arm(args, rank, world, local):
                 args.workload, ps_per_launch / (step_launch_ms * 1e-3), peak),
             "fp64_formulation": formulation_roofline(
                 args.workload, ps_per_launch / (step_launch_ms * 1e-3), peak),
+            "fp64_algorithmic": algorithmic_roofline(
+                args.workload, ps_per_launch / (step_launch_ms * 1e-3), peak),
             "step_share_of_run": step_ms.value / max(run_ms.value, 1e-12),
             "flops_basis": "executed FP64 ops per particle-step (ncu SASS "
                            "dadd+dmul+2*dfma)"}
@@ -873,6 +903,8 @@ def serve_arm(args, rank, world, local):
             "step_kernel_share": step_ms * 1e-3 / served_s,
             "fp64_pipe": pipe_roofline("seir_batched", in_kernel_rate, peak),
             "fp64_formulation": formulation_roofline("seir_batched",
+                                                     in_kernel_rate, peak),
+            "fp64_algorithmic": algorithmic_roofline("seir_batched",
                                                      in_kernel_rate, peak),
             "flops_basis": "executed FP64 ops per particle-step of the "
                            "SEIR step kernel (ncu SASS dadd+dmul+2*dfma)"},
