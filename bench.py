@@ -60,14 +60,16 @@ sys.path.insert(0, str(ROOT))
 
 # Executed FP64 operations (DADD + DMUL + 2 DFMA, per thread) per
 # particle-step of the step+compare kernel, per workload, from the ncu SASS
-# counters of that kernel over a whole likelihood run (summaries under
-# profiles/).  A workload without an entry reports no achieved rate.
-FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 187.3, "seir_batched": 3203.1,
+# counters of that kernel (summaries under profiles/): whole-run averages
+# of an earlier build, scaled by the ratio of the current build's count to
+# that build's at the same observation (one-launch captures).  A workload
+# without an entry reports no achieved rate.
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 180.9, "seir_batched": 3030.4,
                               "ode_batched": 761.7}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
-FP64_PIPE_INST_PER_UNIT = {"sir_batched": 162.7, "seir_batched": 2682.7,
+FP64_PIPE_INST_PER_UNIT = {"sir_batched": 132.7, "seir_batched": 2145.6,
                            "ode_batched": 641.3}
 
 
@@ -126,7 +128,7 @@ def algorithmic_roofline(workload, units_per_s, peak_tflops):
 # launch at observation 200 of the current build, which keeps the state
 # in a per-thread local-memory array); `traffic` is this times the units
 # of one launch.
-DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2447.0,
+DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2442.0,
                        "ode_batched": 40.0}
 
 
