@@ -3,8 +3,9 @@ on the GPU; the CPU oracle then computes groups (or instances, or
 requests) of it.  Groups, instances and sessions are independent, so
 those must agree: log-likelihoods to 1e-12 relative (parallel vs serial
 weight sums), final state and generator words exactly, dopri5 outputs
-within the solver's tolerance (the step controller's pow is each
-platform's own).  Slower than the other tests (a minute or two)."""
+within the solver's tolerance (the GPU solver fuses its stage sums and
+evaluates the controller's powers with the engine's exp and log, so
+its rounding differs from the CPU's).  Slower than the other tests (a minute or two)."""
 
 import ctypes
 
