@@ -88,27 +88,15 @@ DUST2_SAMPLER double binomial_inversion(rng_state& rng, double n, double p,
   return math::quiet_nan();
 }
 
-// log(p / q) of BTRS's acceptance test, computed when first needed ...
-struct btrs_lpq_lazy {
-  double p, q;
-  DUST2_HD double operator()() const {
-    return math::log(p * math::rcp(q));
-  }
-};
-// ... or supplied by a prepared probability (the same value).
-struct btrs_lpq_ready {
-  double lpq;
-  DUST2_HD double operator()() const {
-    return lpq;
-  }
-};
-
 // Divisions by b, us, q and the hat denominator are multiplications by
 // reciprocals (math::rcp); us = 0 (u = -1/2 exactly) is rejected.  Here
-// n p >= 10 and q >= 1/2, so b > 6.8 and v_r > 0.3.
-template <typename LPQ>
+// n p >= 10 and q >= 1/2, so b > 6.8 and v_r > 0.3.  log(p / q) of the
+// acceptance test is given by a prepared probability (lpq_given, always
+// finite there), or, when lpq_given is NaN, computed the first time a
+// candidate needs that test; one body serves both, so a kernel holds one
+// copy of the sampler.
 DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
-                              const LPQ& lpq_of) {
+                                   double lpq_given) {
   const double spq = std::sqrt(n * p * q);
   const double b = std::fma(2.53, spq, 1.15);
   const double a = std::fma(0.01, p, std::fma(0.0248, b, -0.0873));
@@ -139,7 +127,8 @@ DUST2_SAMPLER double binomial_btrs(rng_state& rng, double n, double p, double q,
     }
     if (!have_setup) {
       alpha = std::fma(5.1, inv_b, 2.83) * spq;
-      lpq = lpq_of();
+      lpq = math::is_nan(lpq_given) ? math::log(p * math::rcp(q)) :
+        lpq_given;
       m = math::floor_bits((n + 1.0) * p);
       h = math::log_factorial(m) + math::log_factorial(n - m);
       have_setup = true;
@@ -193,7 +182,7 @@ DUST2_HD double binomial(rng_state& rng, double n, double p) {
     const double s = pp * math::rcp(q);
     x = binomial_inversion(rng, n, pp, q, s, math::log(q));
   } else {
-    x = binomial_btrs(rng, n, pp, q, btrs_lpq_lazy{pp, q});
+    x = binomial_btrs(rng, n, pp, q, math::quiet_nan());
   }
   return flip ? n - x : x;
 }
@@ -250,7 +239,7 @@ DUST2_HD double binomial(rng_state& rng, double n, const binomial_prob& b) {
   if (math::bits_of(n * b.pp) < BITS_TEN) {
     x = binomial_inversion(rng, n, b.pp, b.q, b.s, b.logq);
   } else {
-    x = binomial_btrs(rng, n, b.pp, b.q, btrs_lpq_ready{b.lpq});
+    x = binomial_btrs(rng, n, b.pp, b.q, b.lpq);
   }
   return b.flip ? n - x : x;
 }
