@@ -65,12 +65,12 @@ sys.path.insert(0, str(ROOT))
 # that build's at the same observation (one-launch captures).  A workload
 # without an entry reports no achieved rate.
 FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 180.9, "seir_batched": 3030.4,
-                              "ode_batched": 761.7}
+                              "ode_batched": 596.4}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
 FP64_PIPE_INST_PER_UNIT = {"sir_batched": 132.7, "seir_batched": 2145.6,
-                           "ode_batched": 641.3}
+                           "ode_batched": 373.7}
 
 
 # A second basis for the FP64 roofline, independent of moving work off
@@ -124,12 +124,12 @@ def algorithmic_roofline(workload, units_per_s, peak_tflops):
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per unit of the
-# same kernel, from ncu captures (SIR and dopri5: whole runs; SEIR: one
-# launch at observation 200 of the current build, which keeps the state
-# in a per-thread local-memory array); `traffic` is this times the units
-# of one launch.
+# same kernel, from ncu captures (SIR: a whole run; SEIR: one launch at
+# observation 200, the state in a per-thread local-memory array; dopri5:
+# one launch over all outputs); `traffic` is this times the units of one
+# launch.
 DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2442.0,
-                       "ode_batched": 40.0}
+                       "ode_batched": 36.6}
 
 
 # The CPU path is timed with the oracle's timing build: the host's libm
