@@ -102,13 +102,18 @@ def formulation_roofline(workload, units_per_s, peak_tflops):
 # lgamma counted as calls, not flops), on a sample of each batched
 # workload whose log-likelihoods equal the oracle port's bit for bit
 # (`python -m oracle.opcount.count`: batched SIR groups 1-8, all
-# particles; batched SEIR groups 1-4 at 1024 particles; all observations).
-FP64_ALGORITHMIC_OPS = {"sir_batched": 59.95, "seir_batched": 1738.7}
+# particles; batched SEIR groups 1-4 at 1024 particles; all observations),
+# and, per attempted step, dust2's unfused dopri5 with the sirode system
+# over the same type on instances 1-16384 of the dopri5 workload (outputs
+# and step counts equal to the port's).
+FP64_ALGORITHMIC_OPS = {"sir_batched": 59.95, "seir_batched": 1738.7,
+                        "ode_batched": 443.7}
 ALGORITHMIC_CALLS = {
     "sir_batched": {"exp": 1.66, "log": 1.28, "log_factorial": 1.72,
                     "lgamma": 0.25},
     "seir_batched": {"exp": 44.4, "log": 26.7, "log_factorial": 35.2,
-                     "lgamma": 0.75}}
+                     "lgamma": 0.75},
+    "ode_batched": {"pow": 1.08}}
 
 
 def algorithmic_roofline(workload, units_per_s, peak_tflops):
@@ -1086,6 +1091,8 @@ def ode_arm(args, rank, world, local):
                      "traffic": traffic_per_launch("ode_batched", steps),
                      "fp64_pipe": pipe_roofline("ode_batched",
                                                 steps / (ms * 1e-3), peak),
+                     "fp64_algorithmic": algorithmic_roofline(
+                         "ode_batched", steps / (ms * 1e-3), peak),
                      "flops_basis": "executed FP64 ops per attempted "
                                     "dopri5 step (ncu SASS)"},
     }

@@ -6,9 +6,12 @@ and the binomial sampler restated over an operation-counting real type)
 as a particle filter on a sample of the benchmark's batched workloads,
 checks that its log-likelihoods equal the oracle port's bit for bit (so
 the counted run drew exactly the engine's draws), and prints the counts
-per particle-step:
+per particle-step; and dust2's dopri5 with the sirode system over the
+same type on the batched dopri5 workload, checked equal to the port's
+integration, per attempted step:
 
-    python -m oracle.opcount.count [--workload sir_batched|seir_batched]
+    python -m oracle.opcount.count [--workload sir_batched|seir_batched|
+                                               ode_batched]
 
 Flops: +, -, *, / (a reciprocal counts as one division) and sqrt one
 each, a fused multiply-add two.  Comparisons, floors and calls of exp,
@@ -34,7 +37,7 @@ SRC = HERE / "opcount.cpp"
 LIB = ORACLE / "_build" / "libopcount.so"
 
 OPS = ["add", "mul", "div", "fma", "sqrt", "cmp", "floor", "exp", "log",
-       "log_factorial", "lgamma"]
+       "log_factorial", "lgamma", "pow"]
 N_STATE = {"sir_cases": 4, "seir_age": 96}
 STEPS_PER_OBS = 4
 
@@ -95,6 +98,46 @@ def counted_filter(system, pars, n_particles, dt, times, data, words):
 
 def flops(c):
     return c["add"] + c["mul"] + c["div"] + c["sqrt"] + 2 * c["fma"]
+
+
+def counted_dopri5(pars, times):
+    """sirode instances (packed rows: I0, N, beta, gamma) integrated from 0
+    through `times` by dust2's dopri5 over the counting type; returns
+    (out [time][instance][5], attempted steps per instance, op counts)."""
+    d = ctypes.POINTER(ctypes.c_double)
+    pars = np.ascontiguousarray(pars, dtype=np.float64)
+    times = np.ascontiguousarray(times, dtype=np.float64)
+    n = pars.size // 4
+    out = np.empty(times.size * n * 5)
+    steps = np.empty(n, dtype=np.int64)
+    ops = np.zeros(len(OPS), dtype=np.uint64)
+    _lib().opcount_dopri5_sirode(
+        pars.ctypes.data_as(d), ctypes.c_int(4), ctypes.c_int(n),
+        times.ctypes.data_as(d), ctypes.c_int(times.size),
+        out.ctypes.data_as(d),
+        steps.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+        ops.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    return out, steps, dict(zip(OPS, (int(x) for x in ops)))
+
+
+def count_dopri5(n_instances):
+    """The first n_instances of the batched dopri5 workload, checked
+    against the oracle port (outputs and step counts equal bit for bit);
+    returns op counts per attempted step."""
+    from oracle import pyoracle
+    from dust2_gb300 import workloads
+    w = workloads.sirode_batched(n_instances=n_instances)
+    out, steps, ops = counted_dopri5(w["pars"], w["times"])
+    want, stats = pyoracle.port().ode_simulate(
+        "sirode", w["pars"], n_instances, 1, 0.0, w["times"], 5)
+    if not (np.array_equal(out, want) and
+            np.array_equal(steps, stats[:, 0])):
+        raise RuntimeError("counted dopri5 differs from the port")
+    total = int(steps.sum())
+    return {"attempted_steps": total,
+            "flops_per_step": flops(ops) / total,
+            "per_step": {k: ops[k] / total for k in OPS},
+            "equal_port": True}
 
 
 def oracle_simulate():
@@ -160,8 +203,15 @@ def main():
     args = p.parse_args()
     samples = {"sir_batched": dict(groups=list(range(8))),
                "seir_batched": dict(groups=[0, 1, 2, 3], n_particles=1024)}
-    names = [args.workload] if args.workload else list(samples)
+    names = [args.workload] if args.workload else \
+        list(samples) + ["ode_batched"]
     for name in names:
+        if name == "ode_batched":
+            out = count_dopri5(16384)
+            out["workload"] = name
+            out["sample"] = "instances 1-16384, integrated 0..200"
+            print(json.dumps(out))
+            continue
         s = samples[name]
         out = count(workload(name), **s)
         out["workload"] = name

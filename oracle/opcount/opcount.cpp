@@ -34,6 +34,7 @@
 
 #include "systems/seir_age.hpp"
 #include "systems/sir_cases.hpp"
+#include "systems/sirode.hpp"
 
 namespace {
 
@@ -42,8 +43,9 @@ namespace rnd = dust2gpu::random;
 using rng_t = rnd::rng_state;
 
 // operation counters: [add, mul, div, fma, sqrt, cmp, floor, exp, log,
-// log_factorial, lgamma]
-enum { ADD, MUL, DIV, FMA, SQRT, CMP, FLOOR, EXP, LOG, LFACT, LGAMMA, NOPS };
+// log_factorial, lgamma, pow]
+enum { ADD, MUL, DIV, FMA, SQRT, CMP, FLOOR, EXP, LOG, LFACT, LGAMMA, POW,
+       NOPS };
 std::uint64_t g_ops[NOPS];
 
 struct counted {
@@ -77,6 +79,10 @@ counted log_factorial(counted a) {
   return m::log_factorial(a.v);
 }
 counted lgamma(counted a) { ++g_ops[LGAMMA]; return m::lgamma(a.v); }
+counted pow(counted a, counted b) { ++g_ops[POW]; return std::pow(a.v, b.v); }
+counted max(counted a, counted b) { ++g_ops[CMP]; return std::max(a.v, b.v); }
+counted min(counted a, counted b) { ++g_ops[CMP]; return std::min(a.v, b.v); }
+counted abs(counted a) { return std::abs(a.v); }  // a sign clear
 bool is_nan(counted a) { return std::isnan(a.v); }
 
 // The uniform's centred forms U - 1/2 and 1/2 - |U - 1/2|: two additions.
@@ -452,6 +458,227 @@ double filter_group(const typename SYS::shared_state& sh, int n, double dt,
   return ll;
 }
 
+// ---- dopri5 (dust2's continuous/solver.hpp, as the oracle port) ----
+
+// sirode's right-hand side (dust2gpu/systems/sirode.hpp)
+void sirode_rhs(const dust2gpu::systems::sirode::shared_state& sh,
+                const counted* y, counted* dy) {
+  const counted S = y[0], I = y[1];
+  const counted rate_SI = counted(sh.beta) * S * I / counted(sh.N);
+  const counted rate_IR = counted(sh.gamma) * I;
+  dy[0] = -rate_SI;
+  dy[1] = rate_SI - rate_IR;
+  dy[2] = rate_IR;
+  dy[3] = rate_SI;
+  dy[4] = rate_SI;
+}
+
+// One sirode instance integrated from 0 through `times` with the
+// reference's unfused arithmetic (solver.hpp:96-324, 437-492; controls
+// of control.hpp:11-27 with rtol = atol = 1e-6, step_size_min = DBL_EPSILON,
+// no maximum step), writing the state at each time; returns the number of
+// attempted steps.
+struct dopri5_counted {
+  static constexpr int n = 5;
+  const dust2gpu::systems::sirode::shared_state& sh;
+  counted atol = 1e-6, rtol = 1e-6, factor_safe = 0.9, beta = 0.04,
+    constant = 0.2 - 0.04 * 0.75;
+  double facc1 = 1 / 0.2, facc2 = 1 / 10.0;
+  double step_size_min = std::numeric_limits<double>::epsilon();
+  counted y_next[n], y_stiff[n], k2[n], k3[n], k4[n], k5[n], k6[n];
+  counted dydt[n], c1[n], c2[n], c3[n], c4[n], c5[n];
+  counted t0 = 0.0, h_last = 0.0, step_size = 0.0, error = 0.0;
+  long n_steps = 0, n_accepted = 0;
+
+  static constexpr double C2 = 0.2, C3 = 0.3, C4 = 0.8, C5 = 8.0 / 9.0;
+  static constexpr double A21 = 0.2, A31 = 3.0 / 40.0, A32 = 9.0 / 40.0;
+  static constexpr double A41 = 44.0 / 45.0, A42 = -56.0 / 15.0,
+    A43 = 32.0 / 9.0;
+  static constexpr double A51 = 19372.0 / 6561.0, A52 = -25360.0 / 2187.0,
+    A53 = 64448.0 / 6561.0, A54 = -212.0 / 729.0;
+  static constexpr double A61 = 9017.0 / 3168.0, A62 = -355.0 / 33.0,
+    A63 = 46732.0 / 5247.0, A64 = 49.0 / 176.0, A65 = -5103.0 / 18656.0;
+  static constexpr double A71 = 35.0 / 384.0, A73 = 500.0 / 1113.0,
+    A74 = 125.0 / 192.0, A75 = -2187.0 / 6784.0, A76 = 11.0 / 84.0;
+  static constexpr double E1 = 71.0 / 57600.0, E3 = -71.0 / 16695.0,
+    E4 = 71.0 / 1920.0, E5 = -17253.0 / 339200.0, E6 = 22.0 / 525.0,
+    E7 = -1.0 / 40.0;
+  static constexpr double D1 = -12715105075.0 / 11282082432.0,
+    D3 = 87487479700.0 / 32700410799.0, D4 = -10690763975.0 / 1880347072.0,
+    D5 = 701980252875.0 / 199316789632.0, D6 = -1453857185.0 / 822651844.0,
+    D7 = 69997945.0 / 29380423.0;
+
+  explicit dopri5_counted(const dust2gpu::systems::sirode::shared_state& s)
+    : sh(s) {}
+
+  counted try_step(counted t, counted h, const counted* y) {
+    const counted t_next = t + h;
+    const counted* k1 = dydt;
+    for (int i = 0; i < n; ++i) y_next[i] = y[i] + h * A21 * k1[i];
+    sirode_rhs(sh, y_next, k2);
+    for (int i = 0; i < n; ++i)
+      y_next[i] = y[i] + h * (A31 * k1[i] + A32 * k2[i]);
+    sirode_rhs(sh, y_next, k3);
+    for (int i = 0; i < n; ++i)
+      y_next[i] = y[i] + h * (A41 * k1[i] + A42 * k2[i] + A43 * k3[i]);
+    sirode_rhs(sh, y_next, k4);
+    for (int i = 0; i < n; ++i)
+      y_next[i] = y[i] + h * (A51 * k1[i] + A52 * k2[i] + A53 * k3[i] +
+                              A54 * k4[i]);
+    sirode_rhs(sh, y_next, k5);
+    for (int i = 0; i < n; ++i)
+      y_stiff[i] = y[i] + h * (A61 * k1[i] + A62 * k2[i] + A63 * k3[i] +
+                               A64 * k4[i] + A65 * k5[i]);
+    sirode_rhs(sh, y_stiff, k6);
+    for (int i = 0; i < n; ++i)
+      y_next[i] = y[i] + h * (A71 * k1[i] + A73 * k3[i] + A74 * k4[i] +
+                              A75 * k5[i] + A76 * k6[i]);
+    sirode_rhs(sh, y_next, k2);
+    (void)t_next;
+    for (int i = 0; i < n; ++i)
+      c5[i] = h * (D1 * k1[i] + D3 * k3[i] + D4 * k4[i] + D5 * k5[i] +
+                   D6 * k6[i] + D7 * k2[i]);
+    for (int i = 0; i < n; ++i)
+      k4[i] = h * (E1 * k1[i] + E3 * k3[i] + E4 * k4[i] + E5 * k5[i] +
+                   E6 * k6[i] + E7 * k2[i]);
+    counted err = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const counted sk = k4[i] / (atol + rtol * max(abs(y[i]),
+                                                    abs(y_next[i])));
+      err = err + sk * sk;
+    }
+    return sqrt(err / counted(n));
+  }
+
+  counted step(counted t, counted t_end, counted* y) {
+    bool success = false, reject = false, truncated = false;
+    counted h = step_size;
+    while (!success) {
+      if (h.v < step_size_min || n_steps > 10000) {
+        return std::numeric_limits<double>::quiet_NaN();
+      }
+      truncated = t + h > t_end;
+      if (truncated) {
+        h = t_end - t;
+      }
+      const counted err = try_step(t, h, y);
+      n_steps++;
+      const counted fac11 = pow(err, constant);
+      if (err <= 1.0) {
+        success = true;
+        t0 = t;
+        h_last = h;
+        for (int i = 0; i < n; ++i) {
+          const counted ydiff = y_next[i] - y[i];
+          const counted bspl = h * dydt[i] - ydiff;
+          c1[i] = y[i];
+          c2[i] = ydiff;
+          c3[i] = bspl;
+          c4[i] = -h * k2[i] + ydiff - bspl;
+        }
+        std::copy(k2, k2 + n, dydt);
+        std::copy(y_next, y_next + n, y);
+        n_accepted++;
+        if (!truncated) {
+          const counted fac_old = max(error, 1e-4);
+          counted fac = fac11 / pow(fac_old, beta);
+          fac = max(min(fac / factor_safe, facc1), facc2);
+          const counted h_max =
+            reject ? h : counted(std::numeric_limits<double>::infinity());
+          step_size = min(h / fac, h_max);
+          error = err;
+        }
+      } else {
+        reject = true;
+        h = h / min(facc1, fac11 / factor_safe);
+      }
+    }
+    return truncated ? t_end : t + h;
+  }
+
+  // zero_every of cases_inc (entry 4) every whole time: the reset by
+  // dense-output interpolation (solver.hpp:437-492)
+  void reset_inc(counted t_reset, counted* y) {
+    const counted u = (t_reset - t0) / h_last;
+    const counted v = 1.0 - u;
+    const counted val = c1[4] + u * (c2[4] + v * (c3[4] + u * (c4[4] +
+                                                              v * c5[4])));
+    c4[0] = val;
+    y[4] = y[4] - val;
+  }
+
+  void apply_zero_every(counted t, counted* y) {
+    if (h_last.v == 0) {
+      return;
+    }
+    const counted period = 1.0;
+    const counted nn = floor(t / period);
+    const counted mm = floor(t0 / period);
+    if (nn > mm) {
+      const counted t_reset = nn * period;
+      if (t_reset == t) {
+        y[4] = 0.0;
+      } else {
+        reset_inc(t_reset, y);
+      }
+    }
+  }
+
+  void apply_zero_every_final(counted t, counted* y) {
+    if (h_last.v == 0 || !(h_last.v > 1.0)) {
+      return;
+    }
+    const int nn = static_cast<int>(std::ceil(t.v));
+    const int mm = static_cast<int>(std::ceil(t0.v));
+    if (nn > mm) {
+      reset_inc(static_cast<double>(nn - 1), y);
+    }
+  }
+
+  void initialise(counted t, const counted* y) {
+    counted* f0 = dydt;
+    counted* f1 = k3;
+    counted* y1 = y_next;
+    sirode_rhs(sh, y, f0);
+    counted norm_f = 0.0, norm_y = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const counted sk = atol + rtol * abs(y[i]);
+      norm_f = norm_f + (f0[i] / sk) * (f0[i] / sk);
+      norm_y = norm_y + (y[i] / sk) * (y[i] / sk);
+    }
+    counted h = (norm_f <= 1e-10 || norm_y <= 1e-10) ?
+      counted(1e-6) : sqrt(norm_y / norm_f) * 0.01;
+    for (int i = 0; i < n; ++i) {
+      y1[i] = y[i] + h * f0[i];
+    }
+    sirode_rhs(sh, y1, f1);
+    counted der2 = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const counted sk = atol + rtol * abs(y[i]);
+      der2 = der2 + ((f1[i] - f0[i]) / sk) * ((f1[i] - f0[i]) / sk);
+    }
+    der2 = sqrt(der2) / h;
+    const counted der12 = max(abs(der2), sqrt(norm_f));
+    const counted h1 = (der12 <= 1e-15) ?
+      max(1e-6, abs(h) * 1e-3) : pow(0.01 / der12, 1.0 / 5.0);
+    h = min(100.0 * abs(h), h1);
+    h = max(h, step_size_min * 100);
+    step_size = h;
+    error = 0.0;
+  }
+
+  void run(counted t, counted t_end, counted* y) {
+    while (t < t_end) {
+      apply_zero_every(t, y);
+      t = step(t, t_end, y);
+      if (std::isnan(t.v)) {
+        return;
+      }
+    }
+    apply_zero_every_final(t, y);
+  }
+};
+
 }  // namespace
 
 extern "C" {
@@ -493,6 +720,39 @@ int opcount_filter(const char* name, const double* pars, int n_pars,
     }
     pos += 4 * static_cast<size_t>(2 + n);
   }
+  return 0;
+}
+
+// sirode instances (packed rows of n_pars doubles), each integrated from 0
+// through `times`; out [time][instance][5]; steps: attempted steps per
+// instance; ops: NOPS counters summed over the integration (initialisation
+// included).
+int opcount_dopri5_sirode(const double* pars, int n_pars, int n,
+                          const double* times, int n_times, double* out,
+                          std::int64_t* steps, std::uint64_t* ops) {
+  std::fill(g_ops, g_ops + NOPS, 0);
+  using S = dust2gpu::systems::sirode;
+  for (int k = 0; k < n; ++k) {
+    const auto sh = S::build_shared(pars + static_cast<size_t>(k) * n_pars);
+    typename S::internal_state in{};
+    rnd::rng_state r{};
+    double y0[5];
+    S::initial(0.0, sh, in, r, y0);
+    counted y[5];
+    for (int i = 0; i < 5; ++i) y[i] = y0[i];
+    dopri5_counted sol(sh);
+    sol.initialise(0.0, y);
+    counted t = 0.0;
+    for (int i = 0; i < n_times; ++i) {
+      sol.run(t, times[i], y);
+      t = times[i];
+      for (int q = 0; q < 5; ++q) {
+        out[(static_cast<size_t>(i) * n + k) * 5 + q] = y[q].v;
+      }
+    }
+    steps[k] = sol.n_steps;
+  }
+  std::copy(g_ops, g_ops + NOPS, ops);
   return 0;
 }
 

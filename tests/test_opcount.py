@@ -42,6 +42,21 @@ def test_counted_seir_filter_equals_port(seir):
     assert per["lgamma"] == pytest.approx(0.75)
 
 
+def test_counted_dopri5_equals_port():
+    # dust2's unfused solver over the counting type integrates exactly
+    # as the port does (outputs and step counts), so its counts are those
+    # of the reference arithmetic
+    out = oc.count_dopri5(64)
+    assert out["equal_port"]
+    per = out["per_step"]
+    # six right-hand sides of sirode per attempted step, each with one
+    # division; one square root for the error norm
+    assert per["div"] >= 6
+    assert per["sqrt"] >= 1
+    assert per["fma"] == 0
+    assert 300 < out["flops_per_step"] < 700
+
+
 def test_counts_are_reproducible(sir):
     a = oc.count(sir, [1], n_particles=64, n_obs=10)
     b = oc.count(sir, [1], n_particles=64, n_obs=10)
