@@ -83,7 +83,6 @@ counted pow(counted a, counted b) { ++g_ops[POW]; return std::pow(a.v, b.v); }
 counted max(counted a, counted b) { ++g_ops[CMP]; return std::max(a.v, b.v); }
 counted min(counted a, counted b) { ++g_ops[CMP]; return std::min(a.v, b.v); }
 counted abs(counted a) { return std::abs(a.v); }  // a sign clear
-bool is_nan(counted a) { return std::isnan(a.v); }
 
 // The uniform's centred forms U - 1/2 and 1/2 - |U - 1/2|: two additions.
 void centered(rng_t& rng, counted* u, counted* us) {
