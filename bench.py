@@ -64,12 +64,12 @@ sys.path.insert(0, str(ROOT))
 # of an earlier build, scaled by the ratio of the current build's count to
 # that build's at the same observation (one-launch captures).  A workload
 # without an entry reports no achieved rate.
-FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 180.9, "seir_batched": 3030.4,
+FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 180.9, "seir_batched": 3028.9,
                               "ode_batched": 596.4}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
-FP64_PIPE_INST_PER_UNIT = {"sir_batched": 132.7, "seir_batched": 2145.6,
+FP64_PIPE_INST_PER_UNIT = {"sir_batched": 132.7, "seir_batched": 2155.8,
                            "ode_batched": 373.7}
 
 
@@ -133,7 +133,7 @@ def algorithmic_roofline(workload, units_per_s, peak_tflops):
 # observation 200, the state in a per-thread local-memory array; dopri5:
 # one launch over all outputs); `traffic` is this times the units of one
 # launch.
-DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 2442.0,
+DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 1598.0,
                        "ode_batched": 36.6}
 
 

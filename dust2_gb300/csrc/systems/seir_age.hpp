@@ -25,11 +25,12 @@ struct seir_age {
   static constexpr bool update_in_place = true;
   // The 96 doubles stay in a per-thread array (local memory, cached),
   // with 4 blocks of 128 threads per SM (128 registers).  Measured on
-  // the batched SEIR filter (particle-steps/s): this 118.2M; 3 blocks
-  // 118.0M; two arrays with copies (before in-place updates), 3 blocks
-  // 116.0M; the state in rows of shared memory instead (2 blocks of 99
-  // KB per SM) 107.7M -- occupancy hides the FP64 pipe's latency better
-  // than shared memory saves local-memory traffic.
+  // the batched SEIR filter (particle-steps/s): this 149.5M; 3 blocks
+  // 144.3M; 5 blocks 147.3M.  Earlier builds: two arrays with copies
+  // (before in-place updates) 116.0M against 118.2M in place; the state
+  // in rows of shared memory instead (2 blocks of 99 KB per SM) 107.7M --
+  // occupancy hides the FP64 pipe's latency better than shared memory
+  // saves local-memory traffic.
   static constexpr int min_blocks_per_sm = 4;
   using real_type = double;
   using rng_state_type = random::rng_state;
