@@ -16,11 +16,12 @@
 //
 // GB300's FP64 pipe is the bound, so the FP64 instructions of a step are
 // cut where the rounding may change within the solver's tolerance: the
-// stage sums are fused multiply-add chains over h-scaled weights, and the
+// stage sums are fused multiply-add chains over h-scaled weights, the
 // controller's powers go through the engine's exp and log (integer fixed
-// point).  Everything else (error norm, controller logic, truncation,
-// dense output, zero_every) follows the reference expression by
-// expression.  On 65,536 instances of the batched sirode workload the
+// point), and the error norm's and the controller's divisions are
+// multiplications by the engine's reciprocal.  Everything else
+// (controller logic, truncation, dense output, zero_every) follows the
+// reference expression by expression.  On 65,536 instances of the batched sirode workload the
 // solutions stay within 4e-13 relative of the reference's arithmetic
 // with identical step counts.
 #pragma once
@@ -139,6 +140,14 @@ DUST2_HD double clamp(double x, double lo, double hi) {
   return ref_max(ref_min(x, hi), lo);
 }
 
+// 1/x through the engine's reciprocal (an FP32 seed and two Newton steps,
+// within an ulp) where that is accurate, |x| in [2^-99, 2^99]; a division
+// elsewhere.  Four FP64 instructions instead of a division's sequence.
+DUST2_HD double recip(double x) {
+  const std::uint64_t e = (math::bits_of(x) >> 52) & 0x7ff;
+  return e - (1023 - 99) <= 198 ? math::rcp(x) : 1.0 / x;
+}
+
 template <typename T, int NV>
 struct solver {
   const control_dev& ctl;
@@ -149,6 +158,8 @@ struct solver {
   // Special state after the n_var integrated variables: read by the rhs,
   // carried unchanged through every stage (solver.hpp:236-239, 274-276).
   int n_special = 0;
+  // 1 / n_var for the error norm's mean
+  double inv_n_var = 1.0 / n_var;
 
   DUST2_HD void copy_special(const double* y, double* dst) {
 #pragma unroll
@@ -263,13 +274,13 @@ struct solver {
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
       if (i < n_var) {
-        const double sk = s.k4[i] /
-          std::fma(ctl.rtol, ref_max(fabs(y[i]), fabs(s.y_next[i])),
-                   ctl.atol);
+        const double sk = s.k4[i] *
+          recip(std::fma(ctl.rtol, ref_max(fabs(y[i]), fabs(s.y_next[i])),
+                         ctl.atol));
         err = std::fma(sk, sk, err);
       }
     }
-    return sqrt(err / n_var);
+    return sqrt(err * inv_n_var);
   }
 
   DUST2_HD void update_interpolation(double t, double h, const double* y,
@@ -349,7 +360,7 @@ struct solver {
                                         -ctl.beta * math::log(fac_old)) -
           log_safe;
         const double fac = clamp(math::exp(log_fac), ctl.facc2, ctl.facc1);
-        const double h_new = h / fac;
+        const double h_new = h * recip(fac);
         const double h_max = reject ? h : ctl.step_size_max;
         st.step_size = ref_min(h_new, h_max);
         st.error = err;
@@ -361,8 +372,8 @@ struct solver {
     if (st.n_steps_accepted >= 1) {
       st.n_steps_rejected++;
     }
-    h /= ref_min(ctl.facc1,
-                 math::exp(std::fma(ctl.constant, log_err, -log_safe)));
+    h *= recip(ref_min(ctl.facc1, math::exp(std::fma(ctl.constant, log_err,
+                                                     -log_safe))));
     return 0;
   }
 

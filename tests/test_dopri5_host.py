@@ -2,8 +2,9 @@
 (dust2_gb300/csrc/engine/dopri5.cuh, compiled for the host with nvcc from
 tests/dopri5_host.cu) against the oracle's restatement of dust2's solver
 and against dust2's own fixtures.  The engine evaluates the stage sums as
-fused multiply-add chains and the step-size controller's powers through
-its own exp and log, so it rounds differently from dust2; the contract is
+fused multiply-add chains, the step-size controller's powers through its
+own exp and log and the error norm's divisions through its reciprocal,
+so it rounds differently from dust2; the contract is
 agreement within the solver's tolerance (rtol = atol = 1e-6).  Observed:
 within 4e-13 relative, with the same step counts."""
 
