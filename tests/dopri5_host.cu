@@ -1,11 +1,10 @@
 // The engine's dopri5 solver (dust2_gb300/csrc/engine/dopri5.cuh, host and
 // device code) compiled for the host, so that a CPU test can compare the
 // GPU's arithmetic -- fused stage sums, controller powers through the
-// engine's exp and log, reciprocals for the divisions -- with the oracle's
-// restatement of dust2's
-// solver.  host_ode integrates n instances of a system from time 0
-// through `times`, as k_ode_run does for one particle each: initialise,
-// then one solver run per output time.
+// engine's exp and log, reciprocals for the divisions -- with the
+// oracle's restatement of dust2's solver.  host_ode integrates n
+// instances of a system from time 0 through `times`, as k_ode_run does
+// for one particle each: initialise, then one solver run per output time.
 #include <cstdint>
 #include <string>
 
