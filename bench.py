@@ -65,12 +65,12 @@ sys.path.insert(0, str(ROOT))
 # that build's at the same observation (one-launch captures).  A workload
 # without an entry reports no achieved rate.
 FP64_OPS_PER_PARTICLE_STEP = {"sir_batched": 180.9, "seir_batched": 3028.9,
-                              "ode_batched": 596.4}
+                              "ode_batched": 552.0}
 # FP64-pipe thread instructions (arithmetic, comparisons, conversions) per
 # unit, from the same captures: the pipe's own roofline (every instruction
 # takes one lane-slot; the DFMA peak in TFLOP/s is two flops per slot).
 FP64_PIPE_INST_PER_UNIT = {"sir_batched": 132.7, "seir_batched": 2155.8,
-                           "ode_batched": 373.7}
+                           "ode_batched": 351.5}
 
 
 # A second basis for the FP64 roofline, independent of moving work off
@@ -134,7 +134,7 @@ def algorithmic_roofline(workload, units_per_s, peak_tflops):
 # one launch over all outputs); `traffic` is this times the units of one
 # launch.
 DRAM_BYTES_PER_UNIT = {"sir_batched": 19.4, "seir_batched": 1598.0,
-                       "ode_batched": 36.6}
+                       "ode_batched": 36.5}
 
 
 # The CPU path is timed with the oracle's timing build: the host's libm
