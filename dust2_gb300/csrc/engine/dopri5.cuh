@@ -140,6 +140,18 @@ DUST2_HD double clamp(double x, double lo, double hi) {
   return ref_max(ref_min(x, hi), lo);
 }
 
+// t / period, exactly: for a period that is a power of two (the usual
+// daily reset has period 1) the quotient is t times the exact reciprocal,
+// the same correctly rounded value as the division; other periods divide.
+DUST2_HD double div_period(double t, double period) {
+  const std::uint64_t b = math::bits_of(period);
+  const std::uint64_t e = b >> 52;  // sign and biased exponent
+  if ((b & 0x000fffffffffffffull) == 0 && e >= 2 && e <= 2045) {
+    return t * math::from_bits((2046 - e) << 52);
+  }
+  return t / period;
+}
+
 // 1/x through the engine's reciprocal (an FP32 seed and two Newton steps,
 // within an ulp) where that is accurate, |x| in [2^-99, 2^99]; a division
 // elsewhere.  Four FP64 instructions instead of a division's sequence.
@@ -431,8 +443,9 @@ struct solver {
     }
     for (int e = 0; e < z.n; ++e) {
       const double period = z.period[e];
-      const int n = static_cast<int>(floor(t / period));
-      const int m = static_cast<int>(floor(st.t0 / period));
+      const int n = static_cast<int>(math::floor_bits(div_period(t, period)));
+      const int m =
+        static_cast<int>(math::floor_bits(div_period(st.t0, period)));
       if (n > m) {
         const double t_reset = n * period;
         if (t_reset == t) {
@@ -458,8 +471,8 @@ struct solver {
     for (int e = 0; e < z.n; ++e) {
       const double period = z.period[e];
       if (st.h > period) {
-        const int n = static_cast<int>(ceil(t / period));
-        const int m = static_cast<int>(ceil(st.t0 / period));
+        const int n = static_cast<int>(ceil(div_period(t, period)));
+        const int m = static_cast<int>(ceil(div_period(st.t0, period)));
         if (n > m) {
           const double t_reset = (n - 1) * period;
           interpolate_reset(z, e, t_reset, y, st);
