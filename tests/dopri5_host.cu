@@ -66,6 +66,16 @@ int run(const double* pars, int n_pars, int n, const double* times,
 
 }  // namespace
 
+// The solver's helpers for the CPU tests: t / period as the zero_every
+// check computes it, and 1/x as the error norm and controller compute it.
+extern "C" double host_div_period(double t, double period) {
+  return dp::div_period(t, period);
+}
+
+extern "C" double host_recip(double x) {
+  return dp::recip(x);
+}
+
 extern "C" int host_ode(const char* name, const double* pars, int n_pars,
                         int n, const double* times, int n_times, double* out,
                         std::int64_t* stats, double ssmin, double ssmax,

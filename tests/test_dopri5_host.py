@@ -34,6 +34,10 @@ def host(tmp_path_factory):
          str(ROOT / "tests" / "dopri5_host.cu"), "-o", str(lib)],
         check=True, capture_output=True)
     so = ctypes.CDLL(str(lib))
+    so.host_div_period.restype = ctypes.c_double
+    so.host_div_period.argtypes = [ctypes.c_double, ctypes.c_double]
+    so.host_recip.restype = ctypes.c_double
+    so.host_recip.argtypes = [ctypes.c_double]
     d = ctypes.POINTER(ctypes.c_double)
 
     def run(name, flat, n, times, n_state, critical=()):
@@ -50,6 +54,7 @@ def host(tmp_path_factory):
             crit.ctypes.data_as(d) if crit.size else None, crit.size)
         assert rc == 0
         return out, stats.reshape(n, 3)
+    run.lib = so
     return run
 
 
@@ -85,3 +90,28 @@ def test_dopri5_critical_times_fixture(host):
     got, _ = host("sirode", flat, 1, np.array([50.0]), 5,
                   critical=[10, 20, 30])
     np.testing.assert_allclose(got, g["out"][-5:], rtol=1e-12)
+
+
+def test_period_division_is_exact(host):
+    # the zero_every check's t / period: a multiplication by the exact
+    # reciprocal for powers of two, a division otherwise -- always the
+    # correctly rounded quotient
+    rs = np.random.default_rng(5)
+    ts = np.concatenate([rs.uniform(0, 400, 20000), np.arange(0, 401.0),
+                         rs.uniform(-50, 50, 2000), [0.0, -0.0, 1e-310]])
+    for period in (1.0, 0.5, 0.25, 2.0, 7.0, 2.0 ** -30, 2.0 ** 40, 0.1, 3.0,
+                   -1.0):
+        got = np.array([host.lib.host_div_period(t, period) for t in ts])
+        np.testing.assert_array_equal(got.view(np.uint64),
+                                      (ts / period).view(np.uint64))
+
+
+def test_reciprocal_within_an_ulp(host):
+    rs = np.random.default_rng(6)
+    xs = np.concatenate([10.0 ** rs.uniform(-29, 29, 20000),
+                         -(10.0 ** rs.uniform(-5, 5, 100)),
+                         [1e-300, 1e300, 3.0, 0.1]])
+    got = np.array([host.lib.host_recip(x) for x in xs])
+    want = 1.0 / xs
+    ulp = np.spacing(np.abs(want))
+    assert np.all(np.abs(got - want) <= ulp)
