@@ -20,10 +20,10 @@
 // controller's powers go through the engine's exp and log (integer fixed
 // point), and the error norm's and the controller's divisions are
 // multiplications by the engine's reciprocal.  Everything else
-// (controller logic, truncation, dense output, zero_every) follows the
-// reference expression by expression.  On 65,536 instances of the batched sirode workload the
-// solutions stay within 4e-13 relative of the reference's arithmetic
-// with identical step counts.
+// (controller logic, truncation, dense output, zero_every) computes the
+// reference's values exactly.  On 65,536 instances of the batched sirode
+// workload the solutions stay within 4e-13 relative of the reference's
+// arithmetic with identical step counts.
 #pragma once
 
 #include <cmath>
